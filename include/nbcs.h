@@ -1,0 +1,160 @@
+/*
+ * nbcs.h -- C ABI of the GB300 (sm_103a) flow-map -> FTLE -> ridge library
+ * (libnbcs.so).  Plain pointers and sizes only; every array argument is a
+ * DEVICE pointer unless marked "host".  All calls are asynchronous on the
+ * given CUDA stream (cudaStream_t passed as void*), allocate no memory, and
+ * return an int status (NBCS_OK = 0, negative on error; see nbcs_last_error).
+ *
+ * Each entry point names the reference NumbaCS interface it replaces
+ * (path:line within the NumbaCS project).  In the reference those are
+ * numba-jitted Python functions; the "plugin" is a numba @cfunc RHS whose
+ * address is handed to numbalsoda's dop853.  A host function pointer cannot
+ * run on the GPU, so the RHS is described by the nbcs_flow struct instead and
+ * the right-hand sides are compiled device functions selected by `kind`.
+ */
+#ifndef NBCS_H
+#define NBCS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBCS_ABI_VERSION 1
+
+/* return codes */
+#define NBCS_OK 0
+#define NBCS_ERR_INVALID (-1)     /* bad argument (size, pointer, flow, ...) */
+#define NBCS_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define NBCS_ERR_SCRATCH (-3)     /* scratch buffer missing or too small */
+#define NBCS_ERR_UNSUPPORTED (-4) /* option not supported (e.g. method="lsoda") */
+
+/* per-particle status written by the integrators (int32) */
+#define NBCS_PARTICLE_OK 0
+#define NBCS_PARTICLE_MASKED 1
+#define NBCS_PARTICLE_MAX_STEPS (-2)      /* more than max_steps attempted steps */
+#define NBCS_PARTICLE_STEP_UNDERFLOW (-3) /* 0.1|h| <= |t| * 2.3e-16 */
+#define NBCS_PARTICLE_NONFINITE (-4)      /* error estimate became NaN */
+
+/* flow kinds */
+#define NBCS_FLOW_DOUBLE_GYRE 0 /* flows.py:1144-1178, params[6]  */
+#define NBCS_FLOW_BICKLEY 1     /* flows.py:1180-1245, params[12] */
+#define NBCS_FLOW_SPLINE2D 2    /* flows.py:121-258, params[1]    */
+
+/* integrator precision */
+#define NBCS_PREC_FP64 0  /* every operation in IEEE double, no FMA contraction */
+#define NBCS_PREC_MIXED 1 /* FP32 stages / interpolation, compensated FP32-pair positions */
+
+#define NBCS_MAX_PARAMS 16
+
+/* Replaces the funcptr returned by get_predefined_flow (flows.py:1104-1295)
+ * and get_flow_2D (flows.py:121-258).  For SPLINE2D the coefficient arrays
+ * are the (nt+2, nx+2, ny+2) cubic B-spline coefficients of u and v
+ * interleaved per node: coef_uv[2*node + 0] = u, [2*node + 1] = v. */
+typedef struct nbcs_flow {
+    int32_t kind;      /* NBCS_FLOW_* */
+    int32_t spherical; /* SPLINE2D: 0 planar, 1 lon in [-180,180), 2 lon in [0,360) */
+    int32_t extrap;    /* SPLINE2D: 0 = "constant" (coordinates clamped to the grid box) */
+    int32_t reserved;
+    double r;          /* SPLINE2D spherical: radius (km) for km/h -> deg/h */
+    double grid[9];    /* SPLINE2D: t0,t1,nt, x0,x1,nx, y0,y1,ny (UCGrid tuple) */
+    const double* coef_uv;  /* SPLINE2D FP64 coefficients (device), required */
+    const float* coef_uv32; /* SPLINE2D FP32 copy (device), required for NBCS_PREC_MIXED */
+} nbcs_flow;
+
+/* integrator options; a NULL opts pointer means all defaults */
+typedef struct nbcs_opts {
+    int32_t precision;     /* NBCS_PREC_* (default FP64) */
+    int32_t max_steps;     /* attempted-step limit per particle (default 100000) */
+    int32_t threads_per_block; /* 0 = library default */
+    int32_t blocks_per_sm;     /* 0 = library default */
+    int32_t* stats;        /* optional device (n,3) int32: accepted, rejected, RHS evals */
+    const void* step_model; /* optional learned initial-step model (device), see nbcs_mlp_* */
+} nbcs_opts;
+
+/* Library version / last error message of the calling host thread. */
+int nbcs_abi_version(void);
+const char* nbcs_last_error(void);
+
+/* ---------------------------------------------------------------- flows */
+
+/* get_interp_arrays_2D prefilter (flows.py:9-46 -> interpolation.splines.prefilter,
+ * k=3): natural-BC cubic B-spline coefficients of f (nt,nx,ny) into coef
+ * (nt+2,nx+2,ny+2).  scratch >= nbcs_spline_prefilter_scratch_bytes(). */
+size_t nbcs_spline_prefilter_scratch_bytes(int32_t nt, int32_t nx, int32_t ny);
+int nbcs_spline_prefilter_3d(const double* f, int32_t nt, int32_t nx, int32_t ny,
+                             double* coef, void* scratch, size_t scratch_bytes, void* stream);
+
+/* get_flow_2D coefficient capture (flows.py:156-254 closes over C_eval_u /
+ * C_eval_v): interleave cu, cv (n nodes each) into coef_uv (2n doubles) and,
+ * if coef_uv32 != NULL, an FP32 copy (2n floats). */
+int nbcs_spline_pack_uv(const double* cu, const double* cv, int64_t n, double* coef_uv,
+                        float* coef_uv32, void* stream);
+
+/* One RHS evaluation per point, as the reference @cfunc computes it
+ * (flows.py:1146-1213 and :154-254): ty (n,3) rows (t, x, y) -> dy (n,2).
+ * params: host array of np doubles. */
+int nbcs_eval_rhs(const nbcs_flow* flow, const double* params, int32_t np, const double* ty,
+                  int64_t n, double* dy, int32_t precision, void* stream);
+
+/* ----------------------------------------------------------- integration */
+
+/* flowmap_grid_2D (integration.py:123-182) with method="dop853":
+ * integrate every particle (x[i], y[j]) over solver time
+ * params[0]*[t0, t0+T] with DOP853 (rtol, atol) and write its end position to
+ * flowmap (nx,ny,2).  mask (nx,ny) u8 may be NULL; masked particles are left
+ * 0 with status MASKED.  status (nx,ny) int32 may be NULL. */
+int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T,
+                         const double* x, int32_t nx, const double* y, int32_t ny,
+                         const double* params, int32_t np, double rtol, double atol,
+                         const uint8_t* mask, double* flowmap, int32_t* status,
+                         const nbcs_opts* opts, void* stream);
+
+/* ------------------------------------------------------------ diagnostics */
+
+/* ftle_grid_2D (diagnostics.py:21-65): flowmap (nx,ny,2) -> ftle (nx,ny). */
+int nbcs_ftle_grid_2d(const double* flowmap, int32_t nx, int32_t ny, double T, double dx,
+                      double dy, const uint8_t* mask, double* ftle, void* stream);
+
+/* C_eig_2D (diagnostics.py:200-244): evals (nx,ny,2) ascending, evecs
+ * (nx,ny,2,2) eigenvectors in columns. */
+int nbcs_c_eig_2d(const double* flowmap, int32_t nx, int32_t ny, double dx, double dy,
+                  const uint8_t* mask, double* evals, double* evecs, void* stream);
+
+/* ftle_from_eig (diagnostics.py:247-269) on a strided eigenvalue array:
+ * ftle[k] = log(ev[k*stride]) / (2|T|) if ev > 1 else 0. */
+int nbcs_ftle_from_eig(const double* eigval, int64_t n, int64_t stride, double T,
+                       double* ftle, void* stream);
+
+/* Fused C_eig_2D + ftle_from_eig(eigvals[...,1]) + eigvecs[...,:,1]:
+ * flowmap -> ftle (nx,ny) and evec_max (nx,ny,2) in one pass (the inputs of
+ * ftle_ridge_pts). */
+int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, double T, double dx,
+                      double dy, const uint8_t* mask, double* ftle, double* evec_max,
+                      void* stream);
+
+/* ------------------------------------------------------------- extraction */
+
+/* np.percentile(f, q) as evaluated in the reference's jitted ftle_ridge_pts
+ * (ridges.py:48-51; numba's linear-rank rule), written to *out (device). */
+size_t nbcs_percentile_scratch_bytes(int64_t n);
+int nbcs_percentile(const double* f, int64_t n, double q, double* out, void* scratch,
+                    size_t scratch_bytes, void* stream);
+
+/* ftle_ridge_pts (ridges.py:9-76) and the _ftle_ridges mask (ridges.py:79-154).
+ * Writes mask_out (nx,ny) u8 if not NULL, rpts_full (nx*ny,2) if not NULL
+ * (zeros off the ridge, as _ftle_ridges returns), the row-major compacted
+ * points to pts_out (capacity nx*ny rows) and their count to *n_out
+ * (device int64).  percentile == 0 means threshold 0 (ridges.py:48-49). */
+size_t nbcs_ridge_scratch_bytes(int32_t nx, int32_t ny);
+int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int32_t nx,
+                   const double* y, int32_t ny, double sdd_thresh, double percentile,
+                   uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
+                   void* scratch, size_t scratch_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NBCS_H */

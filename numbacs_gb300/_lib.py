@@ -1,0 +1,83 @@
+"""ctypes binding of libnbcs.so (the C ABI declared in include/nbcs.h).
+
+The library is built in-tree by ``numbacs_gb300.build``.  There is no CPU
+fallback: if the shared library is missing or no CUDA device is present the
+calls raise.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libnbcs.so")
+
+NBCS_OK = 0
+PARTICLE_OK, PARTICLE_MASKED = 0, 1
+PARTICLE_MAX_STEPS, PARTICLE_STEP_UNDERFLOW, PARTICLE_NONFINITE = -2, -3, -4
+FLOW_DOUBLE_GYRE, FLOW_BICKLEY, FLOW_SPLINE2D = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+MAX_PARAMS = 16
+
+
+class NbcsFlow(ctypes.Structure):
+    """Mirror of ``struct nbcs_flow``."""
+    _fields_ = [("kind", ctypes.c_int32), ("spherical", ctypes.c_int32),
+                ("extrap", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("r", ctypes.c_double), ("grid", ctypes.c_double * 9),
+                ("coef_uv", ctypes.c_void_p), ("coef_uv32", ctypes.c_void_p)]
+
+
+class NbcsOpts(ctypes.Structure):
+    """Mirror of ``struct nbcs_opts``."""
+    _fields_ = [("precision", ctypes.c_int32), ("max_steps", ctypes.c_int32),
+                ("threads_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("stats", ctypes.c_void_p), ("step_model", ctypes.c_void_p)]
+
+
+# name -> (restype, argtypes)
+_vp, _d, _i32, _i64, _sz = ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t
+_FP = ctypes.POINTER(NbcsFlow)
+SIGNATURES = {
+    "nbcs_abi_version": (ctypes.c_int, []),
+    "nbcs_last_error": (ctypes.c_char_p, []),
+    "nbcs_spline_prefilter_scratch_bytes": (_sz, [_i32, _i32, _i32]),
+    "nbcs_spline_prefilter_3d": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp, _sz, _vp]),
+    "nbcs_spline_pack_uv": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "nbcs_eval_rhs": (ctypes.c_int, [_FP, _vp, _i32, _vp, _i64, _vp, _i32, _vp]),
+    "nbcs_flowmap_grid_2d": (ctypes.c_int, [_FP, _d, _d, _vp, _i32, _vp, _i32, _vp, _i32, _d, _d,
+                                            _vp, _vp, _vp, ctypes.POINTER(NbcsOpts), _vp]),
+    "nbcs_ftle_grid_2d": (ctypes.c_int, [_vp, _i32, _i32, _d, _d, _d, _vp, _vp, _vp]),
+    "nbcs_c_eig_2d": (ctypes.c_int, [_vp, _i32, _i32, _d, _d, _vp, _vp, _vp, _vp]),
+    "nbcs_ftle_from_eig": (ctypes.c_int, [_vp, _i64, _i64, _d, _vp, _vp]),
+    "nbcs_ftle_evec_2d": (ctypes.c_int, [_vp, _i32, _i32, _d, _d, _d, _vp, _vp, _vp, _vp]),
+    "nbcs_percentile_scratch_bytes": (_sz, [_i64]),
+    "nbcs_percentile": (ctypes.c_int, [_vp, _i64, _d, _vp, _vp, _sz, _vp]),
+    "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
+    "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
+                                      _vp, _sz, _vp]),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libnbcs.so and declare its signatures (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "libnbcs.so is not built (%s); run `python -m numbacs_gb300.build`" % path)
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc):
+    """Raise RuntimeError with the library's message on a non-zero return."""
+    if rc != NBCS_OK:
+        msg = load().nbcs_last_error()
+        raise RuntimeError("libnbcs error %d: %s" % (rc, msg.decode() if msg else ""))

@@ -1,0 +1,75 @@
+// Host-side helpers of the C ABI: error reporting, device queries, flow checks.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <mutex>
+
+#include "nbcs_internal.cuh"
+
+namespace nbcs {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int sm_count()
+{
+    static std::mutex mu;
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    std::lock_guard<std::mutex> lk(mu);
+    if (cache[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 148;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
+int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int precision)
+{
+    if (!flow) return set_error(NBCS_ERR_INVALID, "flow is NULL");
+    if (np < 1 || np > NBCS_MAX_PARAMS || !params)
+        return set_error(NBCS_ERR_INVALID, "params: need 1..%d values, got %d", NBCS_MAX_PARAMS, np);
+    switch (flow->kind) {
+    case NBCS_FLOW_DOUBLE_GYRE:
+        if (np < 6) return set_error(NBCS_ERR_INVALID, "double gyre needs 6 params, got %d", np);
+        break;
+    case NBCS_FLOW_BICKLEY:
+        if (np < 12) return set_error(NBCS_ERR_INVALID, "Bickley jet needs 12 params, got %d", np);
+        break;
+    case NBCS_FLOW_SPLINE2D: {
+        if (flow->spherical < 0 || flow->spherical > 2)
+            return set_error(NBCS_ERR_INVALID, "spherical must be 0, 1 or 2");
+        if (flow->extrap != 0)
+            return set_error(NBCS_ERR_UNSUPPORTED, "only extrap_mode='constant' is supported");
+        for (int d = 0; d < 3; ++d) {
+            double n = flow->grid[3 * d + 2];
+            if (!(n >= 2.0) || !(flow->grid[3 * d + 1] > flow->grid[3 * d]))
+                return set_error(NBCS_ERR_INVALID, "spline grid axis %d needs n >= 2 and b > a", d);
+        }
+        if (!flow->coef_uv) return set_error(NBCS_ERR_INVALID, "spline flow without coefficients");
+        if (precision == NBCS_PREC_MIXED && !flow->coef_uv32)
+            return set_error(NBCS_ERR_INVALID, "mixed precision needs the FP32 coefficient copy");
+        break;
+    }
+    default:
+        return set_error(NBCS_ERR_INVALID, "unknown flow kind %d", flow->kind);
+    }
+    return NBCS_OK;
+}
+
+}  // namespace nbcs
+
+extern "C" int nbcs_abi_version(void) { return NBCS_ABI_VERSION; }
+
+extern "C" const char* nbcs_last_error(void) { return nbcs::g_err; }

@@ -1,0 +1,175 @@
+// FP64 flow-map integration (the plain path) and the RHS probe entry point.
+//
+// Replaces flowmap_grid_2D (integration.py:123-182) with method="dop853":
+// one thread per particle runs the FP64 DOP853 solver of dop853_64.cuh on a
+// device-compiled right-hand side.  Compiled with -fmad=false.
+#include "dop853_64.cuh"
+#include "flows64.cuh"
+#include "flowmap_common.cuh"
+
+namespace nbcs {
+
+template <class Flow>
+__global__ void __launch_bounds__(128)
+flowmap64_kernel(Flow fl, Params P, double ts, double te, const double* __restrict__ x,
+                 const double* __restrict__ y, int nx, int ny, const uint8_t* __restrict__ mask,
+                 double* __restrict__ out, int32_t* __restrict__ status,
+                 int32_t* __restrict__ stats, double rtol, double atol, int nmax)
+{
+    const long n = (long)nx * ny;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        int i = (int)(k / ny), j = (int)(k - (long)i * ny);
+        double yv[2] = {0.0, 0.0};
+        int st = NBCS_PARTICLE_MASKED;
+        Dop853Stats s = {0, 0, 0};
+        if (!(mask && mask[k])) {
+            yv[0] = x[i];
+            yv[1] = y[j];
+            st = dop853_solve64(fl, P, ts, te, yv, rtol, atol, nmax, &s);
+        }
+        reinterpret_cast<double2*>(out)[k] = make_double2(yv[0], yv[1]);
+        if (status) status[k] = st;
+        if (stats) {
+            stats[3 * k] = s.accepted;
+            stats[3 * k + 1] = s.rejected;
+            stats[3 * k + 2] = s.nfcn;
+        }
+    }
+}
+
+template <class Flow>
+__global__ void rhs64_kernel(Flow fl, Params P, const double* __restrict__ ty, long n,
+                             double* __restrict__ dy)
+{
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        double yv[2] = {ty[3 * k + 1], ty[3 * k + 2]}, d[2];
+        fl(ty[3 * k], yv, d, P);
+        dy[2 * k] = d[0];
+        dy[2 * k + 1] = d[1];
+    }
+}
+
+struct Launch64 {
+    const FlowmapArgs* a;
+    template <class Flow>
+    int operator()(const Flow& fl) const
+    {
+        const long n = (long)a->nx * a->ny;
+        int threads = a->threads > 0 ? a->threads : 128;
+        if (threads > 128) threads = 128;
+        long blocks = (n + threads - 1) / threads;
+        if (blocks > (1L << 30)) blocks = 1L << 30;
+        flowmap64_kernel<<<(unsigned)blocks, threads, 0, a->stream>>>(
+            fl, a->P, a->ts, a->te, a->x, a->y, a->nx, a->ny, a->mask, a->out, a->status,
+            a->stats, a->rtol, a->atol, a->nmax);
+        NBCS_LAUNCH_CHECK();
+        return NBCS_OK;
+    }
+};
+
+struct LaunchRhs64 {
+    Params P;
+    const double* ty;
+    long n;
+    double* dy;
+    cudaStream_t stream;
+    template <class Flow>
+    int operator()(const Flow& fl) const
+    {
+        int threads = 128;
+        long blocks = (n + threads - 1) / threads;
+        if (blocks < 1) blocks = 1;
+        rhs64_kernel<<<(unsigned)blocks, threads, 0, stream>>>(fl, P, ty, n, dy);
+        NBCS_LAUNCH_CHECK();
+        return NBCS_OK;
+    }
+};
+
+template <class F>
+static int dispatch64(const nbcs_flow* flow, const F& f)
+{
+    switch (flow->kind) {
+    case NBCS_FLOW_DOUBLE_GYRE: return f(FlowDG64{});
+    case NBCS_FLOW_BICKLEY: return f(FlowBickley64{});
+    default: {
+        SplineGrid g = make_grid(flow->grid);
+        const double2* c = reinterpret_cast<const double2*>(flow->coef_uv);
+        switch (flow->spherical) {
+        case 1: return f(FlowSpline64<1>{g, c, flow->r, flow->extrap});
+        case 2: return f(FlowSpline64<2>{g, c, flow->r, flow->extrap});
+        default: return f(FlowSpline64<0>{g, c, flow->r, flow->extrap});
+        }
+    }
+    }
+}
+
+int launch_flowmap64(const nbcs_flow* flow, const FlowmapArgs& a)
+{
+    return dispatch64(flow, Launch64{&a});
+}
+
+}  // namespace nbcs
+
+using namespace nbcs;
+
+extern "C" int nbcs_eval_rhs(const nbcs_flow* flow, const double* params, int32_t np,
+                             const double* ty, int64_t n, double* dy, int32_t precision,
+                             void* stream)
+{
+    int rc = validate_flow(flow, params, np, precision);
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && (!ty || !dy))) return set_error(NBCS_ERR_INVALID, "eval_rhs: bad arrays");
+    if (n == 0) return NBCS_OK;
+    Params P = {};
+    for (int i = 0; i < np; ++i) P.v[i] = params[i];
+    if (precision == NBCS_PREC_MIXED) return launch_rhs32(flow, P, ty, n, dy, as_stream(stream));
+    return dispatch64(flow, LaunchRhs64{P, ty, (long)n, dy, as_stream(stream)});
+}
+
+extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, const double* x,
+                                    int32_t nx, const double* y, int32_t ny,
+                                    const double* params, int32_t np, double rtol, double atol,
+                                    const uint8_t* mask, double* flowmap, int32_t* status,
+                                    const nbcs_opts* opts, void* stream)
+{
+    nbcs_opts o = {};
+    o.precision = NBCS_PREC_FP64;
+    o.max_steps = 100000;
+    if (opts) {
+        o = *opts;
+        if (o.max_steps <= 0) o.max_steps = 100000;
+    }
+    int rc = validate_flow(flow, params, np, o.precision);
+    if (rc) return rc;
+    if (nx < 0 || ny < 0) return set_error(NBCS_ERR_INVALID, "negative grid size");
+    if ((long)nx * ny == 0) return NBCS_OK;
+    if (!x || !y || !flowmap) return set_error(NBCS_ERR_INVALID, "flowmap_grid_2d: NULL array");
+    if (reinterpret_cast<uintptr_t>(flowmap) & 15)
+        return set_error(NBCS_ERR_INVALID, "flowmap_grid_2d: output must be 16-byte aligned");
+    if (!(rtol > 0.0) || !(atol > 0.0)) return set_error(NBCS_ERR_INVALID, "rtol/atol must be > 0");
+    FlowmapArgs a;
+    for (int i = 0; i < NBCS_MAX_PARAMS; ++i) a.P.v[i] = i < np ? params[i] : 0.0;
+    // t_eval = params[0] * linspace(t0, t0 + T, 2)   (integration.py:164)
+    a.ts = params[0] * t0;
+    a.te = params[0] * (t0 + T);
+    a.x = x;
+    a.y = y;
+    a.nx = nx;
+    a.ny = ny;
+    a.mask = mask;
+    a.out = flowmap;
+    a.status = status;
+    a.stats = o.stats;
+    a.rtol = rtol;
+    a.atol = atol;
+    a.nmax = o.max_steps;
+    a.threads = o.threads_per_block;
+    a.blocks_per_sm = o.blocks_per_sm;
+    a.step_model = o.step_model;
+    a.stream = as_stream(stream);
+    if (o.precision == NBCS_PREC_MIXED) return launch_flowmap32(flow, a);
+    if (o.precision != NBCS_PREC_FP64) return set_error(NBCS_ERR_INVALID, "unknown precision");
+    return launch_flowmap64(flow, a);
+}

@@ -1,0 +1,158 @@
+// FP64 device right-hand sides.
+//
+// These restate the reference's numba @cfunc bodies operation for operation
+// (same operand order, every + - * / separately rounded: this file is only
+// compiled with -fmad=false), so that with the same inputs they produce the
+// same doubles as the CPU oracle apart from the last-bit differences of the
+// transcendental functions.
+//
+//   double gyre   flows.py:1146-1158
+//   Bickley jet   flows.py:1182-1213
+//   spline RHS    flows.py:154-254 (interpolation.eval_spline, k=3)
+#pragma once
+
+#include "nbcs_internal.cuh"
+
+namespace nbcs {
+
+#define NBCS_PI 3.141592653589793
+
+struct FlowDG64 {
+    __device__ __forceinline__ void operator()(double t, const double* y, double* dy,
+                                               const Params& P) const
+    {
+        const double* p = P.v;
+        double tt = p[0] * t;
+        double a = p[2] * sin(p[4] * tt + p[5]);
+        double b = 1.0 - 2.0 * a;
+        double f = a * (y[0] * y[0]) + b * y[0];
+        double df = 2.0 * a * y[0] + b;
+        double sf, cf, sy, cy;
+        sincos(NBCS_PI * f, &sf, &cf);
+        sincos(NBCS_PI * y[1], &sy, &cy);
+        dy[0] = p[0] * (-NBCS_PI * p[1] * sf * cy - p[3] * y[0]);
+        dy[1] = p[0] * (NBCS_PI * p[1] * cf * sy * df - p[3] * y[1]);
+    }
+};
+
+struct FlowBickley64 {
+    __device__ __forceinline__ void operator()(double t, const double* y, double* dy,
+                                               const Params& P) const
+    {
+        const double* p = P.v;
+        double tt = p[0] * t;
+        double Y = y[1] / p[2];
+        double ch = cosh(Y);
+        double sech2 = 1.0 / (ch * ch);
+        double s1 = y[0] - p[9] * tt, s2 = y[0] - p[10] * tt, s3 = y[0] - p[11] * tt;
+        double sn1, cs1, sn2, cs2, sn3, cs3;
+        sincos(p[6] * s1, &sn1, &cs1);
+        sincos(p[7] * s2, &sn2, &cs2);
+        sincos(p[8] * s3, &sn3, &cs3);
+        dy[0] = p[0] * (p[1] * sech2 + 2.0 * p[1] * tanh(Y) * sech2
+                                           * (p[3] * cs1 + p[4] * cs2 + p[5] * cs3));
+        dy[1] = -p[0] * (p[1] * p[2] * sech2
+                         * (p[3] * p[6] * sn1 + p[4] * p[7] * sn2 + p[5] * p[8] * sn3));
+    }
+};
+
+// Python's float modulo (sign of the divisor), as numba evaluates `%`.
+__device__ __forceinline__ double py_fmod(double a, double b)
+{
+    double m = fmod(a, b);
+    if (m != 0.0) {
+        if ((b < 0.0) != (m < 0.0)) m += b;
+    } else {
+        m = copysign(0.0, b);
+    }
+    return m;
+}
+
+__device__ __forceinline__ void bspline_w64(double t, double* w)
+{
+    double t3 = t * t * t, t2 = t * t;
+    w[0] = (-1.0 / 6.0) * t3 + (3.0 / 6.0) * t2 + (-3.0 / 6.0) * t + (1.0 / 6.0);
+    w[1] = (3.0 / 6.0) * t3 + (-6.0 / 6.0) * t2 + (0.0 / 6.0) * t + (4.0 / 6.0);
+    w[2] = (-3.0 / 6.0) * t3 + (3.0 / 6.0) * t2 + (3.0 / 6.0) * t + (1.0 / 6.0);
+    w[3] = (1.0 / 6.0) * t3 + (0.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
+}
+
+// Cell index and fractional offset along axis d; extrap 0 ("constant")
+// clamps the coordinate into [a, b] first.
+__device__ __forceinline__ int spline_locate64(const SplineGrid& g, int d, int extrap,
+                                               double x, double* t)
+{
+    if (extrap == 0) {
+        if (x < g.a[d]) x = g.a[d];
+        if (x > g.b[d]) x = g.b[d];
+    }
+    double u = (x - g.a[d]) * g.dinv[d];
+    double fu = floor(u);
+    int i;
+    if (fu > (double)(g.n[d] - 2)) i = g.n[d] - 2;
+    else if (fu < 0.0) i = 0;
+    else i = (int)fu;
+    *t = u - (double)i;
+    return i;
+}
+
+// Tricubic evaluation of the interleaved (u, v) coefficient block.
+__device__ __forceinline__ void spline_eval_uv64(const SplineGrid& g, const double2* __restrict__ c,
+                                                 int extrap, double t, double x, double y,
+                                                 double* u, double* v)
+{
+    double ft, fx, fy, wt[4], wx[4], wy[4];
+    int it = spline_locate64(g, 0, extrap, t, &ft);
+    int ix = spline_locate64(g, 1, extrap, x, &fx);
+    int iy = spline_locate64(g, 2, extrap, y, &fy);
+    bspline_w64(ft, wt);
+    bspline_w64(fx, wx);
+    bspline_w64(fy, wy);
+    double au = 0.0, av = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        double su = 0.0, sv = 0.0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const double2* row = c + (size_t)(it + a) * g.st + (size_t)(ix + b) * g.sx + iy;
+            double2 r0 = __ldg(row), r1 = __ldg(row + 1), r2 = __ldg(row + 2), r3 = __ldg(row + 3);
+            double bu = wy[0] * r0.x + wy[1] * r1.x + wy[2] * r2.x + wy[3] * r3.x;
+            double bv = wy[0] * r0.y + wy[1] * r1.y + wy[2] * r2.y + wy[3] * r3.y;
+            su += wx[b] * bu;
+            sv += wx[b] * bv;
+        }
+        au += wt[a] * su;
+        av += wt[a] * sv;
+    }
+    *u = au;
+    *v = av;
+}
+
+template <int SPH>
+struct FlowSpline64 {
+    SplineGrid g;
+    const double2* __restrict__ c;
+    double r;
+    int extrap;
+
+    __device__ __forceinline__ void operator()(double t, const double* y, double* dy,
+                                               const Params& P) const
+    {
+        const double* p = P.v;
+        double tt = p[0] * t;
+        double u, v;
+        if (SPH == 1 || SPH == 2) {
+            double xx = SPH == 1 ? py_fmod(y[0] - 180.0, 360.0) - 180.0 : py_fmod(y[0], 360.0);
+            double yy = y[1];
+            spline_eval_uv64(g, c, extrap, tt, xx, yy, &u, &v);
+            dy[0] = p[0] * u * 180.0 / (NBCS_PI * r * cos(yy * NBCS_PI / 180.0));
+            dy[1] = p[0] * v * 180.0 / (NBCS_PI * r);
+        } else {
+            spline_eval_uv64(g, c, extrap, tt, y[0], y[1], &u, &v);
+            dy[0] = p[0] * u;
+            dy[1] = p[0] * v;
+        }
+    }
+};
+
+}  // namespace nbcs

@@ -1,0 +1,241 @@
+// Cauchy-Green / FTLE stencil kernels (HBM-bound).
+//
+//   ftle_grid_2D   diagnostics.py:21-65 (+ utils.gradF_stencil_2D :41-44,
+//                  utils.eigvalsh_max_2D :185-189)
+//   C_eig_2D       diagnostics.py:200-244
+//   ftle_from_eig  diagnostics.py:247-269
+//
+// One thread per grid point; the flow map is read as double2 (16 B per point)
+// and each thread's four neighbours come from the same or adjacent rows, which
+// the L1/L2 caches serve, so DRAM sees ~16 B read + 8 B (FTLE) or +16 B
+// (eigenvector) written per point.  Compiled with -fmad=false: the arithmetic
+// is the reference's, operation for operation.
+#include "nbcs_internal.cuh"
+
+namespace nbcs {
+
+struct Grad {
+    double dxdx, dxdy, dydx, dydy;
+};
+
+__device__ __forceinline__ Grad grad_stencil(const double2* __restrict__ F, long k, int ny,
+                                             double dx, double dy)
+{
+    double2 ip = __ldg(F + k + ny), im = __ldg(F + k - ny);
+    double2 jp = __ldg(F + k + 1), jm = __ldg(F + k - 1);
+    Grad g;
+    g.dxdx = (ip.x - im.x) / (2.0 * dx);
+    g.dxdy = (jp.x - jm.x) / (2.0 * dy);
+    g.dydx = (ip.y - im.y) / (2.0 * dx);
+    g.dydy = (jp.y - jm.y) / (2.0 * dy);
+    return g;
+}
+
+// Symmetric 2x2 eigen-decomposition [[a, b], [b, d]]: the larger eigenvalue by
+// the eigvalsh_max_2D closed form, the smaller one in LAPACK dlaev2's
+// cancellation-free product form, the unit eigenvector of the larger one from
+// the better-conditioned of its two expressions, sign normalised to ex >= 0.
+__device__ __forceinline__ void sym2_eig(double a, double b, double d, double* lmin, double* lmax,
+                                         double* vx, double* vy)
+{
+    double tr = a + d;
+    double disc = sqrt((a - d) * (a - d) + 4.0 * (b * b));
+    double l1 = 0.5 * (tr + disc);
+    double acmx = fabs(a) > fabs(d) ? a : d;
+    double acmn = fabs(a) > fabs(d) ? d : a;
+    double l2 = (l1 != 0.0) ? (acmx / l1) * acmn - (b / l1) * b : 0.5 * (tr - disc);
+    double ex, ey;
+    if (b == 0.0) {
+        if (a >= d) { ex = 1.0; ey = 0.0; }
+        else { ex = 0.0; ey = 1.0; }
+    } else if (a >= d) {
+        ex = l1 - d;
+        ey = b;
+    } else {
+        ex = b;
+        ey = l1 - a;
+    }
+    double nrm = sqrt(ex * ex + ey * ey);
+    ex /= nrm;
+    ey /= nrm;
+    if (ex < 0.0 || (ex == 0.0 && ey < 0.0)) { ex = -ex; ey = -ey; }
+    *lmin = l2;
+    *lmax = l1;
+    *vx = ex;
+    *vy = ey;
+}
+
+__device__ __forceinline__ bool interior(long k, int nx, int ny, int* i, int* j)
+{
+    *i = (int)(k / ny);
+    *j = (int)(k - (long)(*i) * ny);
+    return *i >= 1 && *i < nx - 1 && *j >= 1 && *j < ny - 1;
+}
+
+__global__ void ftle_kernel(const double2* __restrict__ F, int nx, int ny, double scaling,
+                            double dx, double dy, const uint8_t* __restrict__ mask,
+                            double* __restrict__ ftle)
+{
+    const long n = (long)nx * ny;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        int i, j;
+        double out = 0.0;
+        if (interior(k, nx, ny, &i, &j) && !(mask && mask[k])) {
+            Grad g = grad_stencil(F, k, ny, dx, dy);
+            double off = g.dxdx * g.dxdy + g.dydx * g.dydy;
+            double a = g.dxdx * g.dxdx + g.dydx * g.dydx;
+            double d = g.dxdy * g.dxdy + g.dydy * g.dydy;
+            double tr = a + d;
+            double disc = sqrt((a - d) * (a - d) + 4.0 * (off * off));
+            double lmax = 0.5 * (tr + disc);
+            if (lmax > 1.0) out = scaling * log(lmax);
+        }
+        ftle[k] = out;
+    }
+}
+
+__global__ void ceig_kernel(const double2* __restrict__ F, int nx, int ny, double dx, double dy,
+                            const uint8_t* __restrict__ mask, double2* __restrict__ evals,
+                            double2* __restrict__ evecs)
+{
+    const long n = (long)nx * ny;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        int i, j;
+        double2 ev = make_double2(0.0, 0.0);
+        double2 v0 = make_double2(0.0, 0.0), v1 = make_double2(0.0, 0.0);
+        if (interior(k, nx, ny, &i, &j) && !(mask && mask[k])) {
+            Grad g = grad_stencil(F, k, ny, dx, dy);
+            double off = g.dxdx * g.dxdy + g.dydx * g.dydy;
+            double a = g.dxdx * g.dxdx + g.dydx * g.dydx;
+            double d = g.dxdy * g.dxdy + g.dydy * g.dydy;
+            double l0, l1, vx, vy;
+            sym2_eig(a, off, d, &l0, &l1, &vx, &vy);
+            ev = make_double2(l0, l1);
+            v0 = make_double2(-vy, vx);  // row 0: columns v_min, v_max
+            v1 = make_double2(vx, vy);   // row 1
+        }
+        evals[k] = ev;
+        evecs[2 * k] = v0;
+        evecs[2 * k + 1] = v1;
+    }
+}
+
+__global__ void ftle_evec_kernel(const double2* __restrict__ F, int nx, int ny, double den,
+                                 double dx, double dy, const uint8_t* __restrict__ mask,
+                                 double* __restrict__ ftle, double2* __restrict__ evec)
+{
+    const long n = (long)nx * ny;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        int i, j;
+        double f = 0.0;
+        double2 v = make_double2(0.0, 0.0);
+        if (interior(k, nx, ny, &i, &j) && !(mask && mask[k])) {
+            Grad g = grad_stencil(F, k, ny, dx, dy);
+            double off = g.dxdx * g.dxdy + g.dydx * g.dydy;
+            double a = g.dxdx * g.dxdx + g.dydx * g.dydx;
+            double d = g.dxdy * g.dxdy + g.dydy * g.dydy;
+            double l0, l1, vx, vy;
+            sym2_eig(a, off, d, &l0, &l1, &vx, &vy);
+            if (l1 > 1.0) f = log(l1) / den;
+            v = make_double2(vx, vy);
+        }
+        ftle[k] = f;
+        evec[k] = v;
+    }
+}
+
+__global__ void ftle_from_eig_kernel(const double* __restrict__ ev, long n, long stride,
+                                     double den, double* __restrict__ ftle)
+{
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        double e = ev[k * stride];
+        ftle[k] = e > 1.0 ? log(e) / den : 0.0;
+    }
+}
+
+static unsigned grid_for(long n, int threads)
+{
+    long b = (n + threads - 1) / threads;
+    long cap = (long)sm_count() * 16;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace nbcs
+
+using namespace nbcs;
+
+static int check_fm(const double* fm, int32_t nx, int32_t ny)
+{
+    if (nx < 0 || ny < 0) return set_error(NBCS_ERR_INVALID, "negative grid size");
+    if ((long)nx * ny > 0 && !fm) return set_error(NBCS_ERR_INVALID, "flowmap is NULL");
+    if (fm && (reinterpret_cast<uintptr_t>(fm) & 15))
+        return set_error(NBCS_ERR_INVALID, "flowmap must be 16-byte aligned");
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_ftle_grid_2d(const double* flowmap, int32_t nx, int32_t ny, double T,
+                                 double dx, double dy, const uint8_t* mask, double* ftle,
+                                 void* stream)
+{
+    int rc = check_fm(flowmap, nx, ny);
+    if (rc) return rc;
+    long n = (long)nx * ny;
+    if (n == 0) return NBCS_OK;
+    if (!ftle) return set_error(NBCS_ERR_INVALID, "ftle is NULL");
+    double scaling = 1.0 / (2.0 * fabs(T));
+    ftle_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(flowmap), nx, ny, scaling, dx, dy, mask, ftle);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_c_eig_2d(const double* flowmap, int32_t nx, int32_t ny, double dx, double dy,
+                             const uint8_t* mask, double* evals, double* evecs, void* stream)
+{
+    int rc = check_fm(flowmap, nx, ny);
+    if (rc) return rc;
+    long n = (long)nx * ny;
+    if (n == 0) return NBCS_OK;
+    if (!evals || !evecs || ((reinterpret_cast<uintptr_t>(evecs) | reinterpret_cast<uintptr_t>(evals)) & 15))
+        return set_error(NBCS_ERR_INVALID, "evals/evecs NULL or not 16-byte aligned");
+    ceig_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(flowmap), nx, ny, dx, dy, mask,
+        reinterpret_cast<double2*>(evals), reinterpret_cast<double2*>(evecs));
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, double T,
+                                 double dx, double dy, const uint8_t* mask, double* ftle,
+                                 double* evec_max, void* stream)
+{
+    int rc = check_fm(flowmap, nx, ny);
+    if (rc) return rc;
+    long n = (long)nx * ny;
+    if (n == 0) return NBCS_OK;
+    if (!ftle || !evec_max || (reinterpret_cast<uintptr_t>(evec_max) & 15))
+        return set_error(NBCS_ERR_INVALID, "ftle/evec_max NULL or misaligned");
+    ftle_evec_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(flowmap), nx, ny, 2.0 * fabs(T), dx, dy, mask, ftle,
+        reinterpret_cast<double2*>(evec_max));
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_ftle_from_eig(const double* eigval, int64_t n, int64_t stride, double T,
+                                  double* ftle, void* stream)
+{
+    if (n < 0 || stride < 1) return set_error(NBCS_ERR_INVALID, "ftle_from_eig: bad n/stride");
+    if (n == 0) return NBCS_OK;
+    if (!eigval || !ftle) return set_error(NBCS_ERR_INVALID, "ftle_from_eig: NULL array");
+    ftle_from_eig_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(eigval, n, stride,
+                                                                          2.0 * fabs(T), ftle);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}

@@ -1,0 +1,59 @@
+// Internal helpers shared by the libnbcs translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nbcs.h"
+
+namespace nbcs {
+
+// Record a message for nbcs_last_error() (thread-local) and return `code`.
+int set_error(int code, const char* fmt, ...);
+
+#define NBCS_CUDA_TRY(expr)                                                        \
+    do {                                                                           \
+        cudaError_t e_ = (expr);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return ::nbcs::set_error(NBCS_ERR_CUDA, "%s: %s (%s:%d)", #expr,         \
+                                     cudaGetErrorString(e_), __FILE__, __LINE__);  \
+    } while (0)
+
+#define NBCS_LAUNCH_CHECK() NBCS_CUDA_TRY(cudaGetLastError())
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Flow parameters passed by value to kernels (params[0] is the integration
+// direction, as in the reference's @cfunc right-hand sides).
+struct Params {
+    double v[NBCS_MAX_PARAMS];
+};
+
+// Uniform grid of a tricubic spline, with the per-axis reciprocal spacing
+// (n-1)/(b-a) precomputed on the host exactly as the device would.
+struct SplineGrid {
+    double a[3], b[3], dinv[3];
+    int n[3];
+    int sx, st;  // node strides of the (nt+2, nx+2, ny+2) coefficient block
+};
+
+inline SplineGrid make_grid(const double* g)
+{
+    SplineGrid s;
+    for (int d = 0; d < 3; ++d) {
+        s.a[d] = g[3 * d];
+        s.b[d] = g[3 * d + 1];
+        s.n[d] = (int)g[3 * d + 2];
+        s.dinv[d] = (double)(s.n[d] - 1) / (s.b[d] - s.a[d]);
+    }
+    s.sx = s.n[2] + 2;
+    s.st = (s.n[1] + 2) * (s.n[2] + 2);
+    return s;
+}
+
+int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int precision);
+
+}  // namespace nbcs

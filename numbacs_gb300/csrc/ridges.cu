@@ -1,0 +1,487 @@
+// FTLE ridge extraction: exact percentile selection, ridge stencil and
+// order-preserving compaction.
+//
+//   ftle_ridge_pts   extraction/ridges.py:9-76
+//   _ftle_ridges     extraction/ridges.py:79-154 (the mask)
+//   np.percentile    ridges.py:48-51, evaluated by numba inside the jitted
+//                    function: rank = 1 + (n-1)*q/100, value
+//                    lower*(1-m) + upper*m of the order statistics around it.
+//
+// Percentile: radix selection of the k-th smallest double on order-preserving
+// 64-bit keys, 11 bits per pass (6 passes), then one pass for the smallest key
+// above it (the (k+1)-th order statistic).  Each pass is one launch; the last
+// block to finish (atomic ticket, no spinning) picks the digit and resets the
+// histogram for the next pass, so no host round trip is needed.
+//
+// Ridge points: pass 1 evaluates the stencil and writes the mask and one
+// count per block of 2048 points; pass 2 scans the counts; pass 3 ranks the
+// flagged points of each block in row-major order (warp ballots) and writes
+// them compacted, re-evaluating the stencil only at flagged points.
+// Compiled with -fmad=false: the stencil arithmetic is the reference's.
+#include <math.h>
+
+#include "nbcs_internal.cuh"
+
+namespace nbcs {
+
+// ------------------------------------------------------------ percentile
+
+constexpr int kDigitBits = 11;
+constexpr int kBins = 1 << kDigitBits;
+constexpr int kSelThreads = 512;
+
+struct SelState {
+    unsigned long long prefix;  // key bits chosen so far
+    unsigned long long pmask;   // which key bits are chosen
+    unsigned long long next_min;  // smallest key above the k-th key
+    long long rank;             // rank still to find inside the prefix group
+    long long eq;               // elements equal to the k-th key (after the last pass)
+    unsigned int done;          // ticket of finished blocks in the current pass
+    unsigned int nan_count;
+    unsigned int pinf, ninf;
+    double result;
+};
+
+struct SelScratch {
+    unsigned int hist[kBins];
+    SelState st;
+};
+
+__device__ __forceinline__ unsigned long long dkey(double d)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double dkey_decode(unsigned long long k)
+{
+    unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)u);
+}
+
+__global__ void sel_init_kernel(SelScratch* s, long long k)
+{
+    for (int b = threadIdx.x; b < kBins; b += blockDim.x) s->hist[b] = 0;
+    if (threadIdx.x == 0) {
+        s->st.prefix = 0;
+        s->st.pmask = 0;
+        s->st.next_min = ~0ull;
+        s->st.rank = k;
+        s->st.eq = 0;
+        s->st.done = 0;
+        s->st.nan_count = s->st.pinf = s->st.ninf = 0;
+        s->st.result = 0.0;
+    }
+}
+
+// one radix pass: histogram the digit at `shift` of the keys in the current
+// prefix group; the last block selects the digit holding rank `rank`.
+__global__ void __launch_bounds__(kSelThreads)
+sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, int bits, int first)
+{
+    __shared__ unsigned int h[kBins];
+    __shared__ unsigned int cnt[3];
+    __shared__ bool is_last;
+    for (int b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0;
+    if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned long long prefix = s->st.prefix, pmask = s->st.pmask;
+    const unsigned int dmask = (1u << bits) - 1u;
+    unsigned int nn = 0, np = 0, nm = 0;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        double v = f[i];
+        if (isnan(v)) { ++nn; continue; }
+        if (first) {
+            if (v == INFINITY) ++np;
+            else if (v == -INFINITY) ++nm;
+        }
+        unsigned long long key = dkey(v);
+        if ((key & pmask) != prefix) continue;
+        atomicAdd(&h[(unsigned)(key >> shift) & dmask], 1u);
+    }
+    if (first) {
+        if (nn) atomicAdd(&cnt[0], nn);
+        if (np) atomicAdd(&cnt[1], np);
+        if (nm) atomicAdd(&cnt[2], nm);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b <= (int)dmask; b += blockDim.x)
+        if (h[b]) atomicAdd(&s->hist[b], h[b]);
+    if (first && threadIdx.x == 0) {
+        if (cnt[0]) atomicAdd(&s->st.nan_count, cnt[0]);
+        if (cnt[1]) atomicAdd(&s->st.pinf, cnt[1]);
+        if (cnt[2]) atomicAdd(&s->st.ninf, cnt[2]);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(&s->st.done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // last block: find the digit whose cumulative count passes `rank`
+    __shared__ unsigned int part[kSelThreads];
+    const int nb = (int)dmask + 1;
+    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    unsigned int local = 0;
+    for (int q = 0; q < per; ++q) {
+        int b = threadIdx.x * per + q;
+        if (b < nb) local += __ldcg(&s->hist[b]);
+    }
+    part[threadIdx.x] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long rank = s->st.rank, cum = 0;
+        int t = 0;
+        for (; t < (int)blockDim.x; ++t) {
+            if (cum + (long long)part[t] > rank) break;
+            cum += part[t];
+        }
+        int b = t * per;
+        unsigned int hb = 0;
+        for (; b < nb; ++b) {
+            hb = __ldcg(&s->hist[b]);
+            if (cum + (long long)hb > rank) break;
+            cum += hb;
+        }
+        if (b >= nb) b = nb - 1;  // unreachable for a valid rank
+        s->st.rank = rank - cum;
+        s->st.prefix = prefix | ((unsigned long long)b << shift);
+        s->st.pmask = pmask | ((unsigned long long)dmask << shift);
+        s->st.eq = hb;
+        s->st.done = 0;
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kBins; b += blockDim.x) s->hist[b] = 0;
+}
+
+// smallest key strictly above the k-th key; the last block writes the result
+__global__ void __launch_bounds__(kSelThreads)
+sel_final_kernel(const double* __restrict__ f, long n, SelScratch* s, int mode, double m,
+                 double* __restrict__ out)
+{
+    __shared__ unsigned long long wmin[kSelThreads / 32];
+    __shared__ bool is_last;
+    const unsigned long long kk = s->st.prefix;
+    unsigned long long mn = ~0ull;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        double v = f[i];
+        if (isnan(v)) continue;
+        unsigned long long key = dkey(v);
+        if (key > kk && key < mn) mn = key;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long other = __shfl_xor_sync(0xffffffffu, mn, o);
+        mn = other < mn ? other : mn;
+    }
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = mn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mn = wmin[w] < mn ? wmin[w] : mn;
+        if (mn != ~0ull) atomicMin(&s->st.next_min, mn);
+        __threadfence();
+        is_last = (atomicAdd(&s->st.done, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last || threadIdx.x != 0) return;
+    __threadfence();
+    const long long nan_count = (long long)__ldcg(&s->st.nan_count);
+    const long long pinf = (long long)__ldcg(&s->st.pinf), ninf = (long long)__ldcg(&s->st.ninf);
+    double lower = dkey_decode(kk), val;
+    if (nan_count > 0) {
+        val = NAN;
+    } else if (n == 1) {
+        val = lower;
+    } else if (mode == 1) {  // q == 100: maximum
+        val = lower;
+        if ((pinf + ninf) > 0 && !isfinite(val)) val = NAN;
+    } else if (mode == 2) {  // q == 0: minimum, with numba's infinity rules
+        val = lower;
+        if (pinf + ninf > 0) {
+            long long finite = n - (pinf + ninf);
+            if (finite == 0) val = NAN;
+            if (pinf == 1 && n == 2) val = NAN;
+            if (ninf > 1) val = NAN;
+            if (finite == 1 && pinf > 1 && ninf != 1) val = NAN;
+        }
+    } else {
+        unsigned long long up = (s->st.rank + 1 < s->st.eq) ? kk : __ldcg(&s->st.next_min);
+        double upper = (up == ~0ull) ? lower : dkey_decode(up);
+        val = lower * (1.0 - m) + upper * m;
+    }
+    s->st.result = val;
+    if (out) *out = val;
+}
+
+static unsigned sel_grid(long n)
+{
+    long b = (n + kSelThreads * 8 - 1) / (kSelThreads * 8);
+    long cap = (long)sm_count() * 4;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+// enqueue the selection; the result lands in s->st.result (and *out if given)
+static int percentile_enqueue(const double* f, long n, double q, double* out, SelScratch* s,
+                              cudaStream_t st)
+{
+    int mode = 0;
+    long long k = 0;
+    double m = 0.0;
+    if (n == 1) {
+        k = 0;
+    } else if (q == 100.0) {
+        mode = 1;
+        k = n - 1;
+    } else if (q == 0.0) {
+        mode = 2;
+        k = 0;
+    } else {
+        double rank = 1.0 + (double)(n - 1) * (q / 100.0);
+        double fl = floor(rank);
+        m = rank - fl;
+        k = (long long)(fl - 1.0);
+    }
+    sel_init_kernel<<<1, 256, 0, st>>>(s, k);
+    NBCS_LAUNCH_CHECK();
+    unsigned g = sel_grid(n);
+    int shift = 64;
+    for (int pass = 0; shift > 0; ++pass) {
+        int bits = shift >= kDigitBits ? kDigitBits : shift;
+        shift -= bits;
+        sel_pass_kernel<<<g, kSelThreads, 0, st>>>(f, n, s, shift, bits, pass == 0);
+        NBCS_LAUNCH_CHECK();
+    }
+    sel_final_kernel<<<g, kSelThreads, 0, st>>>(f, n, s, mode, m, out);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+// ------------------------------------------------------------ ridges
+
+constexpr int kRidgeThreads = 256;
+constexpr int kRidgeRounds = 8;
+constexpr int kRidgeTile = kRidgeThreads * kRidgeRounds;  // points per block
+
+struct RidgeIn {
+    const double* f;
+    const double2* ev;
+    const double* x;
+    const double* y;
+    int nx, ny;
+    double sdd;
+    const double* fmin_ptr;  // device threshold (percentile) or NULL
+    double fmin_val;         // threshold when fmin_ptr is NULL
+};
+
+// Ridge test at point k = i*ny + j (ridges.py:52-74).  Returns true and the
+// sub-pixel point when (i, j) is a ridge point.
+__device__ __forceinline__ bool ridge_at(const RidgeIn& R, double fmin, double dx, double dy, long k,
+                                         double* px, double* py)
+{
+    const int ny = R.ny;
+    int i = (int)(k / ny), j = (int)(k - (long)i * ny);
+    if (i < 2 || i >= R.nx - 2 || j < 2 || j >= ny - 2) return false;
+    const double* f = R.f;
+    double f0 = f[k];
+    if (!(f0 > fmin)) return false;
+    double fip = f[k + ny], fim = f[k - ny], fjp = f[k + 1], fjm = f[k - 1];
+    double fx = (fip - fim) / (2.0 * dx);
+    double fy = (fjp - fjm) / (2.0 * dy);
+    double fxx = (fip - 2.0 * f0 + fim) / (dx * dx);
+    double fyy = (fjp - 2.0 * f0 + fjm) / (dy * dy);
+    double fxy = (f[k + ny + 1] - f[k + ny - 1] - f[k - ny + 1] + f[k - ny - 1]) / (4.0 * dx * dy);
+    double2 e = R.ev[k];
+    double ex = e.x, ey = e.y;
+    double c2 = ex * (fxx * ex + fxy * ey) + ey * (fxy * ex + fyy * ey);
+    if (!(c2 < -R.sdd)) return false;
+    double t = -(fx * ex + fy * ey) / c2;
+    if (fabs(t * ex) <= dx / 2.0 && fabs(t * ey) <= dy / 2.0) {
+        *px = R.x[i] + t * ex;
+        *py = R.y[j] + t * ey;
+        return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kRidgeThreads)
+ridge_flag_kernel(RidgeIn R, uint8_t* __restrict__ mask, double2* __restrict__ rpts,
+                  unsigned int* __restrict__ block_count)
+{
+    const long n = (long)R.nx * R.ny;
+    const double dx = R.x[1] - R.x[0], dy = R.y[1] - R.y[0];
+    const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
+    const long base = (long)blockIdx.x * kRidgeTile;
+    unsigned int c = 0;
+#pragma unroll 1
+    for (int r = 0; r < kRidgeRounds; ++r) {
+        long k = base + (long)r * kRidgeThreads + threadIdx.x;
+        if (k >= n) break;
+        double px = 0.0, py = 0.0;
+        bool on = ridge_at(R, fmin, dx, dy, k, &px, &py);
+        mask[k] = on ? 1 : 0;
+        if (rpts) rpts[k] = on ? make_double2(px, py) : make_double2(0.0, 0.0);
+        c += on;
+    }
+    __shared__ unsigned int tot;
+    if (threadIdx.x == 0) tot = 0;
+    __syncthreads();
+    if (c) atomicAdd(&tot, c);
+    __syncthreads();
+    if (threadIdx.x == 0) block_count[blockIdx.x] = tot;
+}
+
+// exclusive scan of the per-block counts (one block); total -> *n_out
+__global__ void __launch_bounds__(1024)
+ridge_scan_kernel(const unsigned int* __restrict__ cnt, long nb, unsigned long long* __restrict__ off,
+                  int64_t* __restrict__ n_out)
+{
+    __shared__ unsigned long long part[1024];
+    const long per = (nb + blockDim.x - 1) / blockDim.x;
+    const long b0 = (long)threadIdx.x * per;
+    unsigned long long s = 0;
+    for (long q = 0; q < per; ++q)
+        if (b0 + q < nb) s += cnt[b0 + q];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        unsigned long long v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+    for (long q = 0; q < per; ++q) {
+        if (b0 + q < nb) {
+            off[b0 + q] = run;
+            run += cnt[b0 + q];
+        }
+    }
+    if (threadIdx.x == blockDim.x - 1) *n_out = (int64_t)part[blockDim.x - 1];
+}
+
+__global__ void __launch_bounds__(kRidgeThreads)
+ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
+                     const unsigned long long* __restrict__ off, double2* __restrict__ out)
+{
+    __shared__ unsigned int wsum[kRidgeThreads / 32];
+    const long n = (long)R.nx * R.ny;
+    const double dx = R.x[1] - R.x[0], dy = R.y[1] - R.y[0];
+    const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
+    const long base = (long)blockIdx.x * kRidgeTile;
+    unsigned long long run = off[blockIdx.x];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 1
+    for (int r = 0; r < kRidgeRounds; ++r) {
+        long k = base + (long)r * kRidgeThreads + threadIdx.x;
+        bool on = k < n && mask[k];
+        unsigned int bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        unsigned int before = 0, total = 0;
+        for (int w = 0; w < kRidgeThreads / 32; ++w) {
+            unsigned int v = wsum[w];
+            before += (w < warp) ? v : 0;
+            total += v;
+        }
+        if (on) {
+            double px = 0.0, py = 0.0;
+            ridge_at(R, fmin, dx, dy, k, &px, &py);
+            unsigned int rank = before + __popc(bal & ((1u << lane) - 1u));
+            out[run + rank] = make_double2(px, py);
+        }
+        run += total;
+        __syncthreads();
+    }
+}
+
+}  // namespace nbcs
+
+using namespace nbcs;
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+extern "C" size_t nbcs_percentile_scratch_bytes(int64_t n)
+{
+    (void)n;
+    return align256(sizeof(SelScratch));
+}
+
+extern "C" int nbcs_percentile(const double* f, int64_t n, double q, double* out, void* scratch,
+                               size_t scratch_bytes, void* stream)
+{
+    if (n < 1 || !f || !out) return set_error(NBCS_ERR_INVALID, "percentile: empty input or NULL");
+    if (!(q >= 0.0 && q <= 100.0)) return set_error(NBCS_ERR_INVALID, "percentile: q outside [0, 100]");
+    if (!scratch || scratch_bytes < sizeof(SelScratch))
+        return set_error(NBCS_ERR_SCRATCH, "percentile: scratch needs %zu bytes", sizeof(SelScratch));
+    return percentile_enqueue(f, n, q, out, static_cast<SelScratch*>(scratch), as_stream(stream));
+}
+
+static long ridge_blocks(int32_t nx, int32_t ny)
+{
+    long n = (long)nx * ny;
+    return (n + kRidgeTile - 1) / kRidgeTile;
+}
+
+extern "C" size_t nbcs_ridge_scratch_bytes(int32_t nx, int32_t ny)
+{
+    if (nx < 0 || ny < 0) return 0;
+    long nb = ridge_blocks(nx, ny);
+    return align256(sizeof(SelScratch)) + align256(sizeof(unsigned int) * (size_t)nb) +
+           align256(sizeof(unsigned long long) * (size_t)nb) + align256((size_t)nx * ny);
+}
+
+extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int32_t nx,
+                              const double* y, int32_t ny, double sdd_thresh, double percentile,
+                              uint8_t* mask_out, double* rpts_full, double* pts_out,
+                              int64_t* n_out, void* scratch, size_t scratch_bytes, void* stream)
+{
+    if (nx < 2 || ny < 2) return set_error(NBCS_ERR_INVALID, "ridge_pts: need nx, ny >= 2");
+    if (!f || !evec_max || !x || !y || !pts_out || !n_out)
+        return set_error(NBCS_ERR_INVALID, "ridge_pts: NULL array");
+    if ((reinterpret_cast<uintptr_t>(evec_max) | reinterpret_cast<uintptr_t>(pts_out) |
+         reinterpret_cast<uintptr_t>(rpts_full)) & 15)
+        return set_error(NBCS_ERR_INVALID, "ridge_pts: evec/pts arrays must be 16-byte aligned");
+    if (!(percentile >= 0.0 && percentile <= 100.0))
+        return set_error(NBCS_ERR_INVALID, "ridge_pts: percentile outside [0, 100]");
+    size_t need = nbcs_ridge_scratch_bytes(nx, ny);
+    if (!scratch || scratch_bytes < need)
+        return set_error(NBCS_ERR_SCRATCH, "ridge_pts: scratch needs %zu bytes", need);
+    cudaStream_t st = as_stream(stream);
+    const long n = (long)nx * ny, nb = ridge_blocks(nx, ny);
+    char* p = static_cast<char*>(scratch);
+    SelScratch* sel = reinterpret_cast<SelScratch*>(p);
+    p += align256(sizeof(SelScratch));
+    unsigned int* cnt = reinterpret_cast<unsigned int*>(p);
+    p += align256(sizeof(unsigned int) * (size_t)nb);
+    unsigned long long* off = reinterpret_cast<unsigned long long*>(p);
+    p += align256(sizeof(unsigned long long) * (size_t)nb);
+    uint8_t* mask = mask_out ? mask_out : reinterpret_cast<uint8_t*>(p);
+
+    RidgeIn R;
+    R.f = f;
+    R.ev = reinterpret_cast<const double2*>(evec_max);
+    R.x = x;
+    R.y = y;
+    R.nx = nx;
+    R.ny = ny;
+    R.sdd = sdd_thresh;
+    R.fmin_ptr = nullptr;
+    R.fmin_val = 0.0;
+    if (percentile != 0.0) {  // ridges.py:48-51
+        int rc = percentile_enqueue(f, n, percentile, nullptr, sel, st);
+        if (rc) return rc;
+        R.fmin_ptr = &sel->st.result;
+    }
+    ridge_flag_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
+        R, mask, reinterpret_cast<double2*>(rpts_full), cnt);
+    NBCS_LAUNCH_CHECK();
+    ridge_scan_kernel<<<1, 1024, 0, st>>>(cnt, nb, off, n_out);
+    NBCS_LAUNCH_CHECK();
+    ridge_compact_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
+        R, mask, off, reinterpret_cast<double2*>(pts_out));
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}

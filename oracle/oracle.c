@@ -1,0 +1,636 @@
+/*
+ * CPU oracle (TEST INFRASTRUCTURE ONLY) -- see oracle.h.
+ *
+ * Compiled with -O2 -ffp-contract=off so that every + - * / is a separately
+ * rounded IEEE double operation, in the order written in the reference.
+ *
+ * Reference files followed (paths within the NumbaCS project):
+ *   src/numbacs/flows.py:1146-1158     double gyre RHS, defaults :1162-1172
+ *   src/numbacs/flows.py:1182-1213     Bickley jet RHS, defaults :1217-1238
+ *   src/numbacs/flows.py:9-46          get_interp_arrays_2D (cubic prefilter)
+ *   src/numbacs/flows.py:154-254       get_flow_2D RHS (planar / spherical 1 / 2)
+ *   src/numbacs/integration.py:123-182 flowmap_grid_2D (t_eval scaling, mask, loop)
+ *   src/numbacs/diagnostics.py:21-65   ftle_grid_2D (+ utils.py:41-44, :185-189)
+ *   src/numbacs/diagnostics.py:200-269 C_eig_2D, ftle_from_eig
+ *   src/numbacs/extraction/ridges.py:9-154 ftle_ridge_pts / _ftle_ridges
+ *
+ * Third-party algorithms restated (not present in the reference tree):
+ *   numbalsoda.dop853 -- Hairer & Wanner's dop853 (Dormand-Prince 8(5,3) with
+ *     the dop853 step-size controller and HINIT initial step, default
+ *     constants safe=0.9, fac1=0.333, fac2=6, beta=0, uround=2.3e-16);
+ *   interpolation (EconForge) >= 2.2.6 prefilter/eval_spline -- uniform cubic
+ *     B-spline with natural (zero second derivative) boundary conditions;
+ *   numba's np.percentile -- rank = 1 + (n-1)*q/100, value
+ *     lower*(1-m) + upper*m of the two bracketing order statistics.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../numbacs_gb300/csrc/dop853_tableau.h"
+
+#define PI_D 3.141592653589793
+
+/* ------------------------------------------------------------------ flows */
+
+/* Python float modulo (result has the sign of the divisor). */
+static double py_fmod(double a, double b)
+{
+    double m = fmod(a, b);
+    if (m != 0.0) {
+        if ((b < 0.0) != (m < 0.0)) m += b;
+    } else {
+        m = copysign(0.0, b);
+    }
+    return m;
+}
+
+/* flows.py:1146-1158 */
+static void rhs_double_gyre(double t, const double* y, double* dy, const double* p)
+{
+    double tt = p[0] * t;
+    double a = p[2] * sin(p[4] * tt + p[5]);
+    double b = 1.0 - 2.0 * a;
+    double f = a * (y[0] * y[0]) + b * y[0];
+    double df = 2.0 * a * y[0] + b;
+    dy[0] = p[0] * (-PI_D * p[1] * sin(PI_D * f) * cos(PI_D * y[1]) - p[3] * y[0]);
+    dy[1] = p[0] * (PI_D * p[1] * cos(PI_D * f) * sin(PI_D * y[1]) * df - p[3] * y[1]);
+}
+
+/* flows.py:1182-1213 */
+static void rhs_bickley(double t, const double* y, double* dy, const double* p)
+{
+    double tt = p[0] * t;
+    double Y = y[1] / p[2];
+    double ch = cosh(Y);
+    double sech2 = 1.0 / (ch * ch);
+    double s1 = y[0] - p[9] * tt, s2 = y[0] - p[10] * tt, s3 = y[0] - p[11] * tt;
+    dy[0] = p[0] * (p[1] * sech2
+                    + 2.0 * p[1] * tanh(Y) * sech2
+                          * (p[3] * cos(p[6] * s1) + p[4] * cos(p[7] * s2) + p[5] * cos(p[8] * s3)));
+    dy[1] = -p[0] * (p[1] * p[2] * sech2
+                     * (p[3] * p[6] * sin(p[6] * s1) + p[4] * p[7] * sin(p[7] * s2)
+                        + p[5] * p[8] * sin(p[8] * s3)));
+}
+
+/* uniform cubic B-spline basis at fractional offset t (rows of the
+ * standard B-spline matrix applied to [t^3, t^2, t, 1]) */
+static void bspline_weights(double t, double w[4])
+{
+    double t3 = t * t * t, t2 = t * t;
+    w[0] = (-1.0 / 6.0) * t3 + (3.0 / 6.0) * t2 + (-3.0 / 6.0) * t + (1.0 / 6.0);
+    w[1] = (3.0 / 6.0) * t3 + (-6.0 / 6.0) * t2 + (0.0 / 6.0) * t + (4.0 / 6.0);
+    w[2] = (-3.0 / 6.0) * t3 + (3.0 / 6.0) * t2 + (3.0 / 6.0) * t + (1.0 / 6.0);
+    w[3] = (1.0 / 6.0) * t3 + (0.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
+}
+
+/* cell index and fractional offset along one axis (a, b, n); extrap 0
+ * clamps the coordinate into [a, b] first */
+static int spline_locate(double a, double b, int n, int extrap, double x, double* t)
+{
+    if (extrap == 0) {
+        if (x < a) x = a;
+        if (x > b) x = b;
+    }
+    double dinv = (double)(n - 1) / (b - a);
+    double u = (x - a) * dinv;
+    double fu = floor(u);
+    int i;
+    if (fu > (double)(n - 2)) i = n - 2;
+    else if (fu < 0.0) i = 0;
+    else i = (int)fu;
+    *t = u - (double)i;
+    return i;
+}
+
+double orc_eval_spline_3d(const double* g, const double* c, int extrap,
+                          double t, double x, double y)
+{
+    int nt = (int)g[2], nx = (int)g[5], ny = (int)g[8];
+    int sx = ny + 2, st = (nx + 2) * (ny + 2);
+    double ft, fx, fy, wt[4], wx[4], wy[4];
+    int it = spline_locate(g[0], g[1], nt, extrap, t, &ft);
+    int ix = spline_locate(g[3], g[4], nx, extrap, x, &fx);
+    int iy = spline_locate(g[6], g[7], ny, extrap, y, &fy);
+    bspline_weights(ft, wt);
+    bspline_weights(fx, wx);
+    bspline_weights(fy, wy);
+    double acc = 0.0;
+    for (int a = 0; a < 4; ++a) {
+        double sa = 0.0;
+        for (int b = 0; b < 4; ++b) {
+            const double* row = c + (size_t)(it + a) * st + (size_t)(ix + b) * sx + iy;
+            double sb = wy[0] * row[0] + wy[1] * row[1] + wy[2] * row[2] + wy[3] * row[3];
+            sa += wx[b] * sb;
+        }
+        acc += wt[a] * sa;
+    }
+    return acc;
+}
+
+/* flows.py:154-254 */
+static void rhs_spline(const orc_flow* fl, double t, const double* y, double* dy, const double* p)
+{
+    double tt = p[0] * t;
+    if (fl->spherical == 1 || fl->spherical == 2) {
+        double xx = fl->spherical == 1 ? py_fmod(y[0] - 180.0, 360.0) - 180.0 : py_fmod(y[0], 360.0);
+        double yy = y[1];
+        double u = orc_eval_spline_3d(fl->grid, fl->cu, fl->extrap, tt, xx, yy);
+        double v = orc_eval_spline_3d(fl->grid, fl->cv, fl->extrap, tt, xx, yy);
+        dy[0] = p[0] * u * 180.0 / (PI_D * fl->r * cos(yy * PI_D / 180.0));
+        dy[1] = p[0] * v * 180.0 / (PI_D * fl->r);
+    } else {
+        double u = orc_eval_spline_3d(fl->grid, fl->cu, fl->extrap, tt, y[0], y[1]);
+        double v = orc_eval_spline_3d(fl->grid, fl->cv, fl->extrap, tt, y[0], y[1]);
+        dy[0] = p[0] * u;
+        dy[1] = p[0] * v;
+    }
+}
+
+void orc_rhs(const orc_flow* flow, double t, const double* y, double* dy, const double* p)
+{
+    switch (flow->kind) {
+    case ORC_FLOW_DOUBLE_GYRE: rhs_double_gyre(t, y, dy, p); break;
+    case ORC_FLOW_BICKLEY: rhs_bickley(t, y, dy, p); break;
+    default: rhs_spline(flow, t, y, dy, p); break;
+    }
+}
+
+/* ------------------------------------------------------- spline prefilter */
+
+/* Natural-BC interpolation along one line of n samples (stride s):
+ *   c[-1] - 2c[0] + c[1] = 0,  (c[i-1] + 4c[i] + c[i+1])/6 = f[i],
+ *   c[n-2] - 2c[n-1] + c[n] = 0.
+ * The end rows give c[0] = f[0], c[n-1] = f[n-1]; the interior is a
+ * (1,4,1) tridiagonal system solved by forward elimination / back
+ * substitution.  `cw` is scratch of length n. */
+static void prefilter_line(const double* f, long fs, int n, double* c, long cs, double* cw)
+{
+    /* c has n+2 entries, c[0] <-> node -1 */
+    if (n == 1) {
+        c[0] = c[cs] = c[2 * cs] = f[0];
+        return;
+    }
+    double c0 = f[0], cn1 = f[(long)(n - 1) * fs];
+    /* unknowns c_1..c_{n-2}; rhs_i = 6 f_i minus known neighbours */
+    int m = n - 2;
+    double* d = cw; /* modified diagonal */
+    double* r = cw + n; /* modified rhs */
+    for (int k = 0; k < m; ++k) {
+        int i = k + 1;
+        double rhs = 6.0 * f[(long)i * fs];
+        if (k == 0) rhs -= c0;
+        if (k == m - 1) rhs -= cn1;
+        if (k == 0) {
+            d[k] = 4.0;
+            r[k] = rhs;
+        } else {
+            double w = 1.0 / d[k - 1];
+            d[k] = 4.0 - w;
+            r[k] = rhs - w * r[k - 1];
+        }
+    }
+    double next = 0.0;
+    for (int k = m - 1; k >= 0; --k) {
+        double v = (k == m - 1) ? r[k] / d[k] : (r[k] - next) / d[k];
+        c[(long)(k + 2) * cs] = v;
+        next = v;
+    }
+    c[1 * cs] = c0;
+    c[(long)n * cs] = cn1;
+    double c1 = (n > 2) ? c[2 * cs] : cn1;
+    double cn2 = (n > 2) ? c[(long)(n - 1) * cs] : c0;
+    c[0] = 2.0 * c0 - c1;
+    c[(long)(n + 1) * cs] = 2.0 * cn1 - cn2;
+}
+
+int orc_prefilter_3d(const double* f, int nt, int nx, int ny, double* coef)
+{
+    if (nt < 1 || nx < 1 || ny < 1) return -1;
+    int NT = nt + 2, NX = nx + 2, NY = ny + 2;
+    size_t nmax = (size_t)(NT > NX ? (NT > NY ? NT : NY) : (NX > NY ? NX : NY));
+    double* cw = (double*)malloc(sizeof(double) * 2 * nmax);
+    double* tmp = (double*)malloc(sizeof(double) * (size_t)NT * nx * ny);
+    double* tmp2 = (double*)malloc(sizeof(double) * (size_t)NT * NX * ny);
+    if (!cw || !tmp || !tmp2) { free(cw); free(tmp); free(tmp2); return -2; }
+    /* axis t: f (nt,nx,ny) -> tmp (NT,nx,ny) */
+    for (int ix = 0; ix < nx; ++ix)
+        for (int iy = 0; iy < ny; ++iy)
+            prefilter_line(f + (size_t)ix * ny + iy, (long)nx * ny, nt,
+                           tmp + (size_t)ix * ny + iy, (long)nx * ny, cw);
+    /* axis x: tmp (NT,nx,ny) -> tmp2 (NT,NX,ny) */
+    for (int it = 0; it < NT; ++it)
+        for (int iy = 0; iy < ny; ++iy)
+            prefilter_line(tmp + (size_t)it * nx * ny + iy, ny, nx,
+                           tmp2 + (size_t)it * NX * ny + iy, ny, cw);
+    /* axis y: tmp2 (NT,NX,ny) -> coef (NT,NX,NY) */
+    for (int it = 0; it < NT; ++it)
+        for (int ix = 0; ix < NX; ++ix)
+            prefilter_line(tmp2 + ((size_t)it * NX + ix) * ny, 1, ny,
+                           coef + ((size_t)it * NX + ix) * NY, 1, cw);
+    free(cw); free(tmp); free(tmp2);
+    return 0;
+}
+
+/* ------------------------------------------------------------- DOP853 */
+
+static double dmax(double a, double b) { return a > b ? a : b; }
+static double dmin(double a, double b) { return a < b ? a : b; }
+static double dsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+
+#define N2 2
+
+/* HINIT of dop853 (initial step-size guess, iord = 8). */
+static double hinit(const orc_flow* fl, const double* p, double x, const double* y,
+                    double posneg, const double* f0, double* f1, double hmax,
+                    double rtol, double atol)
+{
+    double dnf = 0.0, dny = 0.0, sk, sqr, h, der2, der12, h1, y1[N2];
+    for (int i = 0; i < N2; ++i) {
+        sk = atol + rtol * fabs(y[i]);
+        sqr = f0[i] / sk;
+        dnf += sqr * sqr;
+        sqr = y[i] / sk;
+        dny += sqr * sqr;
+    }
+    if (dnf <= 1.0e-10 || dny <= 1.0e-10) h = 1.0e-6;
+    else h = sqrt(dny / dnf) * 0.01;
+    h = dmin(h, hmax);
+    h = dsign(h, posneg);
+    for (int i = 0; i < N2; ++i) y1[i] = y[i] + h * f0[i];
+    orc_rhs(fl, x + h, y1, f1, p);
+    der2 = 0.0;
+    for (int i = 0; i < N2; ++i) {
+        sk = atol + rtol * fabs(y[i]);
+        sqr = (f1[i] - f0[i]) / sk;
+        der2 += sqr * sqr;
+    }
+    der2 = sqrt(der2) / h;
+    der12 = dmax(fabs(der2), sqrt(dnf));
+    if (der12 <= 1.0e-15) h1 = dmax(1.0e-6, fabs(h) * 1.0e-3);
+    else h1 = pow(0.01 / der12, 1.0 / 8.0);
+    h = dmin(100.0 * fabs(h), dmin(h1, hmax));
+    return dsign(h, posneg);
+}
+
+int orc_dop853(const orc_flow* fl, const double* p, double x, double xend,
+               double* y, double rtol, double atol, int nmax, int32_t* stats3)
+{
+    const double uround = 2.3e-16, safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
+    double k1[N2], k2[N2], k3[N2], k4[N2], k5[N2], k6[N2], k7[N2], k8[N2], k9[N2], k10[N2];
+    double yy1[N2];
+    double facold = 1.0e-4, expo1 = 1.0 / 8.0 - beta * 0.2;
+    double facc1 = 1.0 / fac1, facc2 = 1.0 / fac2;
+    double posneg = dsign(1.0, xend - x);
+    double hmax, h, hnew, xph, err, err2, deno, fac, fac11, sk, erri, sqr;
+    int last = 0, reject = 0, nstep = 0, naccpt = 0, nrejct = 0, nfcn = 0, status = ORC_OK;
+
+    if (xend == x) {
+        if (stats3) { stats3[0] = 0; stats3[1] = 0; stats3[2] = 0; }
+        return ORC_OK;
+    }
+    orc_rhs(fl, x, y, k1, p);
+    hmax = fabs(xend - x);
+    h = hinit(fl, p, x, y, posneg, k1, k2, hmax, rtol, atol);
+    nfcn += 2;
+
+    for (;;) {
+        if (nstep > nmax) { status = ORC_MAX_STEPS; break; }
+        if (0.1 * fabs(h) <= fabs(x) * uround) { status = ORC_STEP_UNDERFLOW; break; }
+        if ((x + 1.01 * h - xend) * posneg > 0.0) {
+            h = xend - x;
+            last = 1;
+        }
+        nstep++;
+        for (int i = 0; i < N2; ++i) yy1[i] = y[i] + h * DP853_A_2_1 * k1[i];
+        orc_rhs(fl, x + DP853_C_2 * h, yy1, k2, p);
+        for (int i = 0; i < N2; ++i) yy1[i] = y[i] + h * (DP853_A_3_1 * k1[i] + DP853_A_3_2 * k2[i]);
+        orc_rhs(fl, x + DP853_C_3 * h, yy1, k3, p);
+        for (int i = 0; i < N2; ++i) yy1[i] = y[i] + h * (DP853_A_4_1 * k1[i] + DP853_A_4_3 * k3[i]);
+        orc_rhs(fl, x + DP853_C_4 * h, yy1, k4, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_5_1 * k1[i] + DP853_A_5_3 * k3[i] + DP853_A_5_4 * k4[i]);
+        orc_rhs(fl, x + DP853_C_5 * h, yy1, k5, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_6_1 * k1[i] + DP853_A_6_4 * k4[i] + DP853_A_6_5 * k5[i]);
+        orc_rhs(fl, x + DP853_C_6 * h, yy1, k6, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_7_1 * k1[i] + DP853_A_7_4 * k4[i] + DP853_A_7_5 * k5[i]
+                                 + DP853_A_7_6 * k6[i]);
+        orc_rhs(fl, x + DP853_C_7 * h, yy1, k7, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_8_1 * k1[i] + DP853_A_8_4 * k4[i] + DP853_A_8_5 * k5[i]
+                                 + DP853_A_8_6 * k6[i] + DP853_A_8_7 * k7[i]);
+        orc_rhs(fl, x + DP853_C_8 * h, yy1, k8, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_9_1 * k1[i] + DP853_A_9_4 * k4[i] + DP853_A_9_5 * k5[i]
+                                 + DP853_A_9_6 * k6[i] + DP853_A_9_7 * k7[i] + DP853_A_9_8 * k8[i]);
+        orc_rhs(fl, x + DP853_C_9 * h, yy1, k9, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_10_1 * k1[i] + DP853_A_10_4 * k4[i] + DP853_A_10_5 * k5[i]
+                                 + DP853_A_10_6 * k6[i] + DP853_A_10_7 * k7[i] + DP853_A_10_8 * k8[i]
+                                 + DP853_A_10_9 * k9[i]);
+        orc_rhs(fl, x + DP853_C_10 * h, yy1, k10, p);
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_11_1 * k1[i] + DP853_A_11_4 * k4[i] + DP853_A_11_5 * k5[i]
+                                 + DP853_A_11_6 * k6[i] + DP853_A_11_7 * k7[i] + DP853_A_11_8 * k8[i]
+                                 + DP853_A_11_9 * k9[i] + DP853_A_11_10 * k10[i]);
+        orc_rhs(fl, x + DP853_C_11 * h, yy1, k2, p);
+        xph = x + h;
+        for (int i = 0; i < N2; ++i)
+            yy1[i] = y[i] + h * (DP853_A_12_1 * k1[i] + DP853_A_12_4 * k4[i] + DP853_A_12_5 * k5[i]
+                                 + DP853_A_12_6 * k6[i] + DP853_A_12_7 * k7[i] + DP853_A_12_8 * k8[i]
+                                 + DP853_A_12_9 * k9[i] + DP853_A_12_10 * k10[i] + DP853_A_12_11 * k2[i]);
+        orc_rhs(fl, xph, yy1, k3, p);
+        nfcn += 11;
+        for (int i = 0; i < N2; ++i) {
+            k4[i] = DP853_B_1 * k1[i] + DP853_B_6 * k6[i] + DP853_B_7 * k7[i] + DP853_B_8 * k8[i]
+                    + DP853_B_9 * k9[i] + DP853_B_10 * k10[i] + DP853_B_11 * k2[i] + DP853_B_12 * k3[i];
+            k5[i] = y[i] + h * k4[i];
+        }
+        /* error estimation: 5th-order estimate combined with the 3rd-order one */
+        err = 0.0;
+        err2 = 0.0;
+        for (int i = 0; i < N2; ++i) {
+            sk = atol + rtol * dmax(fabs(y[i]), fabs(k5[i]));
+            erri = k4[i] - DP853_BHH1 * k1[i] - DP853_BHH2 * k9[i] - DP853_BHH3 * k3[i];
+            sqr = erri / sk;
+            err2 += sqr * sqr;
+            erri = DP853_E5_1 * k1[i] + DP853_E5_6 * k6[i] + DP853_E5_7 * k7[i] + DP853_E5_8 * k8[i]
+                   + DP853_E5_9 * k9[i] + DP853_E5_10 * k10[i] + DP853_E5_11 * k2[i]
+                   + DP853_E5_12 * k3[i];
+            sqr = erri / sk;
+            err += sqr * sqr;
+        }
+        deno = err + 0.01 * err2;
+        if (deno <= 0.0) deno = 1.0;
+        err = fabs(h) * err * sqrt(1.0 / (deno * (double)N2));
+        if (isnan(err)) { status = ORC_NONFINITE; break; }
+        /* new step size, fac1 <= hnew/h <= fac2 */
+        fac11 = pow(err, expo1);
+        fac = fac11 / pow(facold, beta);
+        fac = dmax(facc2, dmin(facc1, fac / safe));
+        hnew = h / fac;
+        if (err <= 1.0) {
+            facold = dmax(err, 1.0e-4);
+            naccpt++;
+            orc_rhs(fl, xph, k5, k4, p);
+            nfcn++;
+            for (int i = 0; i < N2; ++i) {
+                k1[i] = k4[i];
+                y[i] = k5[i];
+            }
+            x = xph;
+            if (last) break;
+            if (fabs(hnew) > hmax) hnew = posneg * hmax;
+            if (reject) hnew = posneg * dmin(fabs(hnew), fabs(h));
+            reject = 0;
+        } else {
+            hnew = h / dmin(facc1, fac11 / safe);
+            reject = 1;
+            if (naccpt >= 1) nrejct++;
+            last = 0;
+        }
+        h = hnew;
+    }
+    if (stats3) { stats3[0] = naccpt; stats3[1] = nrejct; stats3[2] = nfcn; }
+    return status;
+}
+
+int orc_flowmap_grid_2d(const orc_flow* fl, double t0, double T,
+                        const double* x, int nx, const double* y, int ny,
+                        const double* params, int np, double rtol, double atol,
+                        const uint8_t* mask, double* out, int32_t* status,
+                        int32_t* stats, int nmax, int nthreads)
+{
+    (void)np;
+    /* t_eval = params[0] * linspace(t0, t0 + T, 2)   (integration.py:164) */
+    double ts = params[0] * t0;
+    double te = params[0] * (t0 + T);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int i = 0; i < nx; ++i) {
+        for (int j = 0; j < ny; ++j) {
+            size_t k = (size_t)i * ny + j;
+            if (mask && mask[k]) {
+                out[2 * k] = 0.0;
+                out[2 * k + 1] = 0.0;
+                if (status) status[k] = ORC_MASKED;
+                if (stats) { stats[3 * k] = 0; stats[3 * k + 1] = 0; stats[3 * k + 2] = 0; }
+                continue;
+            }
+            double yv[2] = {x[i], y[j]};
+            int st = orc_dop853(fl, params, ts, te, yv, rtol, atol, nmax, stats ? stats + 3 * k : 0);
+            out[2 * k] = yv[0];
+            out[2 * k + 1] = yv[1];
+            if (status) status[k] = st;
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------ FTLE */
+
+/* diagnostics.py:21-65 with utils.gradF_stencil_2D (:41-44) and
+ * utils.eigvalsh_max_2D (:185-189) */
+void orc_ftle_grid_2d(const double* F, int nx, int ny, double T, double dx, double dy,
+                      const uint8_t* mask, double* ftle)
+{
+    double scaling = 1.0 / (2.0 * fabs(T));
+    memset(ftle, 0, sizeof(double) * (size_t)nx * ny);
+#ifdef _OPENMP
+#pragma omp parallel for
+#endif
+    for (int i = 1; i < nx - 1; ++i) {
+        for (int j = 1; j < ny - 1; ++j) {
+            size_t k = (size_t)i * ny + j;
+            if (mask && mask[k]) continue;
+            double dxdx = (F[2 * (k + ny)] - F[2 * (k - ny)]) / (2.0 * dx);
+            double dxdy = (F[2 * (k + 1)] - F[2 * (k - 1)]) / (2.0 * dy);
+            double dydx = (F[2 * (k + ny) + 1] - F[2 * (k - ny) + 1]) / (2.0 * dx);
+            double dydy = (F[2 * (k + 1) + 1] - F[2 * (k - 1) + 1]) / (2.0 * dy);
+            double off = dxdx * dxdy + dydx * dydy;
+            double a = dxdx * dxdx + dydx * dydx;
+            double d = dxdy * dxdy + dydy * dydy;
+            double tr = a + d;
+            double disc = sqrt((a - d) * (a - d) + 4.0 * (off * off));
+            double lmax = 0.5 * (tr + disc);
+            if (lmax > 1.0) ftle[k] = scaling * log(lmax);
+        }
+    }
+}
+
+/* Symmetric 2x2 eigen-decomposition [[a,b],[b,d]], ascending eigenvalues.
+ * lmax uses the same closed form as eigvalsh_max_2D; lmin is taken from the
+ * product of the eigenvalues in the cancellation-free form used by LAPACK's
+ * dlaev2 (the reference calls LAPACK through np.linalg.eigh).  The unit
+ * eigenvector of lmax is built from the larger of the two stable
+ * expressions; its sign is normalised to a non-negative x component. */
+static void sym2_eig(double a, double b, double d, double* lmin, double* lmax,
+                     double* vx, double* vy)
+{
+    double tr = a + d;
+    double disc = sqrt((a - d) * (a - d) + 4.0 * (b * b));
+    double l1 = 0.5 * (tr + disc);
+    double acmx = fabs(a) > fabs(d) ? a : d;
+    double acmn = fabs(a) > fabs(d) ? d : a;
+    double l2 = (l1 != 0.0) ? (acmx / l1) * acmn - (b / l1) * b : 0.5 * (tr - disc);
+    double ex, ey;
+    if (b == 0.0) {
+        if (a >= d) { ex = 1.0; ey = 0.0; }
+        else { ex = 0.0; ey = 1.0; }
+    } else if (a >= d) {
+        ex = l1 - d;
+        ey = b;
+    } else {
+        ex = b;
+        ey = l1 - a;
+    }
+    double nrm = sqrt(ex * ex + ey * ey);
+    ex /= nrm;
+    ey /= nrm;
+    if (ex < 0.0 || (ex == 0.0 && ey < 0.0)) { ex = -ex; ey = -ey; }
+    *lmin = l2;
+    *lmax = l1;
+    *vx = ex;
+    *vy = ey;
+}
+
+/* diagnostics.py:200-244: evals (nx,ny,2) ascending, evecs (nx,ny,2,2) with
+ * eigenvectors in columns (evecs[...,:,1] belongs to the larger eigenvalue) */
+void orc_c_eig_2d(const double* F, int nx, int ny, double dx, double dy,
+                  const uint8_t* mask, double* evals, double* evecs)
+{
+    memset(evals, 0, sizeof(double) * (size_t)nx * ny * 2);
+    memset(evecs, 0, sizeof(double) * (size_t)nx * ny * 4);
+#ifdef _OPENMP
+#pragma omp parallel for
+#endif
+    for (int i = 1; i < nx - 1; ++i) {
+        for (int j = 1; j < ny - 1; ++j) {
+            size_t k = (size_t)i * ny + j;
+            if (mask && mask[k]) continue;
+            double dxdx = (F[2 * (k + ny)] - F[2 * (k - ny)]) / (2.0 * dx);
+            double dxdy = (F[2 * (k + 1)] - F[2 * (k - 1)]) / (2.0 * dy);
+            double dydx = (F[2 * (k + ny) + 1] - F[2 * (k - ny) + 1]) / (2.0 * dx);
+            double dydy = (F[2 * (k + 1) + 1] - F[2 * (k - 1) + 1]) / (2.0 * dy);
+            double off = dxdx * dxdy + dydx * dydy;
+            double a = dxdx * dxdx + dydx * dydx;
+            double d = dxdy * dxdy + dydy * dydy;
+            double l0, l1, vx, vy;
+            sym2_eig(a, off, d, &l0, &l1, &vx, &vy);
+            evals[2 * k] = l0;
+            evals[2 * k + 1] = l1;
+            /* columns: v_min = (-vy, vx), v_max = (vx, vy) */
+            evecs[4 * k + 0] = -vy; /* [0][0] */
+            evecs[4 * k + 1] = vx;  /* [0][1] */
+            evecs[4 * k + 2] = vx;  /* [1][0] */
+            evecs[4 * k + 3] = vy;  /* [1][1] */
+        }
+    }
+}
+
+/* diagnostics.py:247-269 */
+void orc_ftle_from_eig(const double* ev, int64_t n, double T, double* ftle)
+{
+    double den = 2.0 * fabs(T);
+    for (int64_t k = 0; k < n; ++k) ftle[k] = ev[k] > 1.0 ? log(ev[k]) / den : 0.0;
+}
+
+/* -------------------------------------------------------- percentile */
+
+static int cmp_double(const void* a, const void* b)
+{
+    double x = *(const double*)a, y = *(const double*)b;
+    return (x > y) - (x < y);
+}
+
+/* numba's np.percentile for a NaN-free input and 0 < q < 100:
+ * rank = 1 + (n-1)*(q/100); f = floor(rank); m = rank - f;
+ * lower/upper = order statistics k = f-1 and f; value = lower*(1-m) + upper*m.
+ * q == 100 returns the maximum, q == 0 the minimum; any NaN -> NaN. */
+double orc_percentile(const double* f, int64_t n, double q)
+{
+    if (n <= 0) return NAN;
+    for (int64_t k = 0; k < n; ++k)
+        if (isnan(f[k])) return NAN;
+    if (n == 1) return f[0];
+    double* s = (double*)malloc(sizeof(double) * (size_t)n);
+    memcpy(s, f, sizeof(double) * (size_t)n);
+    qsort(s, (size_t)n, sizeof(double), cmp_double);
+    double val;
+    int64_t pinf = 0, ninf = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        if (s[k] == INFINITY) ++pinf;
+        else if (s[k] == -INFINITY) ++ninf;
+    }
+    if (q == 100.0) {
+        val = s[n - 1];
+        if (pinf + ninf > 0 && !isfinite(val)) val = NAN;
+    } else if (q == 0.0) {
+        val = s[0];
+        if (pinf + ninf > 0) {
+            int64_t finite = n - (pinf + ninf);
+            if (finite == 0) val = NAN;
+            if (pinf == 1 && n == 2) val = NAN;
+            if (ninf > 1) val = NAN;
+            if (finite == 1 && pinf > 1 && ninf != 1) val = NAN;
+        }
+    } else {
+        double rank = 1.0 + (double)(n - 1) * (q / 100.0);
+        double fl = floor(rank);
+        double m = rank - fl;
+        int64_t k = (int64_t)(fl - 1.0);
+        double lower = s[k], upper = s[k + 1 < n ? k + 1 : n - 1];
+        val = lower * (1.0 - m) + upper * m;
+    }
+    free(s);
+    return val;
+}
+
+/* ------------------------------------------------------------ ridges */
+
+/* extraction/ridges.py:79-154 (_ftle_ridges); ftle_ridge_pts (:9-76) is the
+ * row-major compaction of rpts_full over mask_out. */
+void orc_ridge_field(const double* f, const double* ev, const double* x, int nx,
+                     const double* y, int ny, double sdd_thresh, double f_min,
+                     uint8_t* mask_out, double* rpts)
+{
+    double dx = x[1] - x[0];
+    double dy = y[1] - y[0];
+    memset(mask_out, 0, (size_t)nx * ny);
+    memset(rpts, 0, sizeof(double) * 2 * (size_t)nx * ny);
+#ifdef _OPENMP
+#pragma omp parallel for
+#endif
+    for (int i = 2; i < nx - 2; ++i) {
+        for (int j = 2; j < ny - 2; ++j) {
+            size_t k = (size_t)i * ny + j;
+            double f0 = f[k];
+            if (!(f0 > f_min)) continue;
+            double fx = (f[k + ny] - f[k - ny]) / (2.0 * dx);
+            double fy = (f[k + 1] - f[k - 1]) / (2.0 * dy);
+            double fxx = (f[k + ny] - 2.0 * f[k] + f[k - ny]) / (dx * dx);
+            double fyy = (f[k + 1] - 2.0 * f[k] + f[k - 1]) / (dy * dy);
+            double fxy = (f[k + ny + 1] - f[k + ny - 1] - f[k - ny + 1] + f[k - ny - 1])
+                         / (4.0 * dx * dy);
+            double ex = ev[2 * k], ey = ev[2 * k + 1];
+            double c2 = ex * (fxx * ex + fxy * ey) + ey * (fxy * ex + fyy * ey);
+            if (c2 < -sdd_thresh) {
+                double t = -(fx * ex + fy * ey) / c2;
+                if (fabs(t * ex) <= dx / 2.0 && fabs(t * ey) <= dy / 2.0) {
+                    rpts[2 * k] = x[i] + t * ex;
+                    rpts[2 * k + 1] = y[j] + t * ey;
+                    mask_out[k] = 1;
+                }
+            }
+        }
+    }
+}

@@ -1,0 +1,109 @@
+"""Extract the reference's golden vectors for the flow-map -> FTLE -> ridge path
+into ``tests/golden/reference_fixtures.npz``.
+
+Sources (paths within the NumbaCS project; the reference itself cannot be
+imported here because numba / numbalsoda / interpolation are absent):
+
+  tests/testing_data/fm.npy         flowmap_grid_2D, double gyre 21x11, t0=0, T=8
+                                    (tests/test_integration.py:55-64)
+  tests/testing_data/ftle.npy       ftle_grid_2D(fm, 8, 0.1, 0.1)  (tests/test_diagnostics.py:82-96)
+  tests/testing_data/Cevals.npy,    C_eig_2D(fm, 0.1, 0.1)           (tests/test_diagnostics.py:133-150)
+  tests/testing_data/Cevecs.npy
+  tests/testing_data/ridge_pts.npy  ftle_ridge_pts(ftle, Cevecs[...,1], x, y) (tests/test_extraction.py:6-12)
+  tests/testing_data/ridges.pkl     ftle_ridges(ftle, Cevecs[...,1], x, y)    (tests/test_extraction.py:14-20)
+  tests/test_flows.py literals      spline coefficients Cu/Cv (:74-133), spline values at 27
+                                    points (:208-229), double-gyre and Bickley velocities
+                                    at the same 27 points (:315-357)
+
+The ``.npy`` files are read with ``allow_pickle=False``; the ``.pkl`` file is read
+with an unpickler that only admits numpy array reconstruction; the test-source
+literals are read with ``ast`` (never executed).
+
+Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+"""
+import ast
+import io
+import os
+import pickle
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class _NumpyOnlyUnpickler(pickle.Unpickler):
+    _ALLOWED = {
+        ("numpy.core.multiarray", "_reconstruct"), ("numpy._core.multiarray", "_reconstruct"),
+        ("numpy", "ndarray"), ("numpy", "dtype"),
+        ("numpy.core.multiarray", "scalar"), ("numpy._core.multiarray", "scalar"),
+    }
+
+    def find_class(self, module, name):
+        if (module, name) in self._ALLOWED:
+            mod = __import__(module, fromlist=[name])
+            return getattr(mod, name)
+        raise pickle.UnpicklingError("refusing %s.%s" % (module, name))
+
+
+def _load_pkl(path):
+    with open(path, "rb") as fh:
+        return _NumpyOnlyUnpickler(io.BytesIO(fh.read())).load()
+
+
+def _eval_literal(node):
+    """Evaluate np.array([...]) / tuples / nested lists without executing code."""
+    if isinstance(node, ast.Call):
+        fn = node.func
+        if isinstance(fn, ast.Attribute) and fn.attr == "array":
+            return np.array(_eval_literal(node.args[0]), dtype=np.float64)
+        raise ValueError("unexpected call")
+    if isinstance(node, ast.Tuple):
+        return tuple(_eval_literal(e) for e in node.elts)
+    return ast.literal_eval(node)
+
+
+def _test_literals(path):
+    tree = ast.parse(open(path).read())
+    out = {}
+    for fn in tree.body:
+        if not isinstance(fn, ast.FunctionDef):
+            continue
+        for node in ast.walk(fn):
+            if (isinstance(node, ast.Assign) and len(node.targets) == 1
+                    and isinstance(node.targets[0], ast.Name)
+                    and node.targets[0].id.endswith("_expected")):
+                try:
+                    out[(fn.name, node.targets[0].id)] = _eval_literal(node.value)
+                except (ValueError, SyntaxError):
+                    pass
+    return out
+
+
+def main(ref_root):
+    td = os.path.join(ref_root, "tests", "testing_data")
+    arrays = {}
+    for name in ("fm", "ftle", "Cevals", "Cevecs", "ridge_pts"):
+        arrays[name] = np.load(os.path.join(td, name + ".npy"), allow_pickle=False)
+    ridges = _load_pkl(os.path.join(td, "ridges.pkl"))
+    arrays["n_ridges"] = np.array(len(ridges))
+    for k, r in enumerate(ridges):
+        arrays["ridges_%d" % k] = np.asarray(r)
+    lit = _test_literals(os.path.join(ref_root, "tests", "test_flows.py"))
+    arrays["spline_Cu"] = lit[("test_get_interp_arrays_2D", "Cu_expected")]
+    arrays["spline_Cv"] = lit[("test_get_interp_arrays_2D", "Cv_expected")]
+    vu, vv = lit[("test_get_callable_2D", "veli_expected")]
+    arrays["spline_vel"] = np.stack([vu, vv], axis=1)
+    du, dv = lit[("test_get_predefined_callable_dg", "veli_expected")]
+    arrays["dg_vel"] = np.stack([du, dv], axis=1)
+    bu, bv = lit[("test_get_predefined_callable_bickley", "veli_expected")]
+    arrays["bickley_vel"] = np.stack([bu, bv], axis=1)
+    out = os.path.join(HERE, "reference_fixtures.npz")
+    np.savez_compressed(out, **arrays)
+    for k, v in sorted(arrays.items()):
+        print("%-14s %s %s" % (k, np.shape(v), np.asarray(v).dtype))
+    print("wrote", out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NBCS_REFERENCE_ROOT", "/root/reference"))

@@ -1,0 +1,173 @@
+"""CUDA flow-map integration against the golden vectors and the CPU oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import apply_mask
+
+pytestmark = pytest.mark.gpu
+
+
+def test_rhs_golden(nb, golden, orc):
+    from test_oracle_golden import _spline_case
+    t, xs, u, v, pts = _spline_case()
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    dg = nb.flows.eval_rhs(fl, pts[:, 0], pts[:, 1:], p)
+    assert np.allclose(dg, golden["dg_vel"])
+    ref = np.array([orc.rhs(orc.double_gyre(), q[0], q[1:], p) for q in pts])
+    np.testing.assert_allclose(dg, ref, rtol=1e-15, atol=1e-16)
+    fb, pb, _ = nb.get_predefined_flow("bickley_jet")
+    bj = nb.flows.eval_rhs(fb, pts[:, 0], pts[:, 1:], pb)
+    assert np.allclose(bj, golden["bickley_vel"])
+    np.testing.assert_allclose(
+        bj, np.array([orc.rhs(orc.bickley_jet(), q[0], q[1:], pb) for q in pts]), rtol=1e-14,
+        atol=1e-15)
+    # mixed-precision right-hand sides agree to FP32 accuracy
+    dg32 = nb.flows.eval_rhs(fl, pts[:, 0], pts[:, 1:], p, precision="mixed")
+    np.testing.assert_allclose(dg32, dg, rtol=0, atol=2e-6)
+    bj32 = nb.flows.eval_rhs(fb, pts[:, 0], pts[:, 1:], pb, precision="mixed")
+    np.testing.assert_allclose(bj32, bj, rtol=0, atol=2e-5)
+
+
+def test_spline_prefilter_golden(nb, golden, orc):
+    from test_oracle_golden import _spline_case
+    t, xs, u, v, pts = _spline_case()
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, xs, xs, u, v)
+    assert np.allclose(Cu, golden["spline_Cu"]) and np.allclose(Cv, golden["spline_Cv"])
+    fl = nb.get_flow_2D(grid, Cu, Cv)
+    vel = nb.flows.eval_rhs(fl, pts[:, 0], pts[:, 1:], np.array([1.0]))
+    assert np.allclose(vel, golden["spline_vel"])
+    # bit-identical to the oracle's prefilter on a ragged random block
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal((7, 13, 5))
+    c = nb.flows._prefilter(torch.from_numpy(f).cuda()).cpu().numpy()
+    assert np.array_equal(c, orc.prefilter_3d(f))
+    # degenerate axes (n = 2) and a long axis
+    for shape in [(2, 2, 2), (3, 2, 300), (2, 1000, 3)]:
+        f = rng.standard_normal(shape)
+        c = nb.flows._prefilter(torch.from_numpy(f).cuda()).cpu().numpy()
+        assert np.array_equal(c, orc.prefilter_3d(f)), shape
+
+
+def test_flowmap_golden(nb, golden, coords_dg, mask_dg):
+    x, y = coords_dg
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    fm = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p)
+    assert np.allclose(fm.astype(np.float32), golden["fm"])
+    fmm = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, mask=mask_dg)
+    assert np.allclose(fmm.astype(np.float32), apply_mask(golden["fm"], mask_dg))
+
+
+def _compare(nb_out, orc_out, nb_stats, orc_stats, extent, name):
+    """Parity: step sequences identical for (almost) all particles; positions
+    within 1e-6 of the domain extent everywhere."""
+    same_steps = np.all(nb_stats == orc_stats, axis=-1)
+    err = np.abs(nb_out - orc_out).max(axis=-1)
+    frac_same = same_steps.mean()
+    assert frac_same >= 0.999, (name, frac_same)
+    assert err.max() <= 1e-6 * extent, (name, err.max())
+    # where the step sequence matched, agreement is to rounding
+    assert err[same_steps].max() <= 1e-9 * extent, (name, err[same_steps].max())
+
+
+def test_flowmap_parity_double_gyre(nb, orc):
+    x, y = np.linspace(0, 2, 101), np.linspace(0, 1, 51)
+    fl, p, _ = nb.get_predefined_flow("double_gyre", int_direction=-1.0)
+    fm, st, stats = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, return_status=True,
+                                       return_stats=True)
+    ofm, ost, ostats = orc.flowmap_grid_2D(orc.double_gyre(), 0.0, -10.0, x, y, p,
+                                           return_status=True)
+    assert (st == 0).all() and (ost == 0).all()
+    _compare(fm, ofm, stats, ostats, 2.0, "dg")
+
+
+def test_flowmap_parity_bickley(nb, orc):
+    fl, p, dom = nb.get_predefined_flow("bickley_jet")
+    x = np.linspace(dom[0][0], dom[0][1], 61)
+    y = np.linspace(dom[1][0], dom[1][1], 31)
+    fm, stats = nb.flowmap_grid_2D(fl, 0.0, 6.0, x, y, p, return_stats=True)
+    ofm, _, ostats = orc.flowmap_grid_2D(orc.bickley_jet(), 0.0, 6.0, x, y, p, return_status=True)
+    _compare(fm, ofm, stats, ostats, dom[0][1] - dom[0][0], "bickley")
+
+
+def _small_geo(orc, seed=0):
+    from numbacs_gb300 import workloads as W
+    t, lon, lat = W.geo_grid()
+    # a reduced sample grid keeps the oracle run to seconds
+    t, lon, lat = t[::4], lon[::4], lat[::4]
+    _, _, _, U, V = W.geo_velocity(seed, t=t, lon=lon, lat=lat, nmodes=64)
+    return t, lon, lat, U, V
+
+
+@pytest.mark.parametrize("spherical", [0, 1, 2])
+def test_flowmap_parity_spline(nb, orc, spherical):
+    t, lon, lat, U, V = _small_geo(orc)
+    if spherical == 2:
+        lon = lon + 180.0  # lon in [80, 215] for the [0, 360) convention
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, U, V)
+    og, oCu, oCv = orc.get_interp_arrays_2D(t, lon, lat, U, V)
+    assert np.array_equal(Cu, oCu) and np.array_equal(Cv, oCv)
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=spherical)
+    of = orc.spline_flow(og, oCu, oCv, spherical=spherical)
+    xf = np.linspace(lon[0], lon[-1], 41)
+    yf = np.linspace(lat[0], lat[-1], 21)
+    p = np.array([-1.0])
+    fm, stats = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, return_stats=True)
+    ofm, _, ostats = orc.flowmap_grid_2D(of, 180.0, -72.0, xf, yf, p, return_status=True)
+    _compare(fm, ofm, stats, ostats, lon[-1] - lon[0], "spline%d" % spherical)
+
+
+def test_flowmap_torch_in_torch_out(nb, coords_dg):
+    x, y = coords_dg
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    xt, yt = torch.tensor(x, device="cuda"), torch.tensor(y, device="cuda")
+    out = torch.empty((len(x), len(y), 2), dtype=torch.float64, device="cuda")
+    fm = nb.flowmap_grid_2D(fl, 0.0, 8.0, xt, yt, p, out=out)
+    assert fm is out and fm.is_cuda
+    assert np.array_equal(fm.cpu().numpy(), nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p))
+
+
+def test_flowmap_deterministic(nb):
+    x, y = np.linspace(0, 2, 64), np.linspace(0, 1, 32)
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    for prec in ("fp64", "mixed"):
+        a = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, precision=prec)
+        b = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, precision=prec)
+        assert np.array_equal(a, b), prec
+
+
+def test_mixed_precision_vs_converged_truth(nb, orc):
+    # the mixed path is judged against an FP64 solution converged to 1e-12
+    x, y = np.linspace(0, 2, 81), np.linspace(0, 1, 41)
+    fl, p, _ = nb.get_predefined_flow("double_gyre", int_direction=-1.0)
+    truth = orc.flowmap_grid_2D(orc.double_gyre(), 0.0, -10.0, x, y, p, rtol=1e-12, atol=1e-14)
+    plain = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, rtol=1e-8, atol=1e-10)
+    mixed = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, rtol=1e-8, atol=1e-10, precision="mixed")
+    e_plain = np.abs(plain - truth).max()
+    e_mixed = np.abs(mixed - truth).max()
+    assert e_plain <= 2e-6
+    assert e_mixed <= 2e-6, e_mixed  # 1e-6 of the domain extent (2)
+    # at the default tolerance both controllers stay within the same bound of each other
+    m6 = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, precision="mixed")
+    p6 = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p)
+    assert np.median(np.abs(m6 - p6)) < 1e-7
+
+
+def test_status_codes(nb):
+    x, y = np.linspace(0.1, 1.9, 8), np.linspace(0.1, 0.9, 4)
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    # step limit injected from the host
+    fm, st = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, max_steps=1, return_status=True)
+    assert (st == -2).all()
+    with pytest.warns(RuntimeWarning):
+        nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, max_steps=1)
+    # NaN parameters -> NaN error estimate -> NONFINITE (no hang, no fault)
+    pn = p.copy()
+    pn[1] = np.nan
+    for prec in ("fp64", "mixed"):
+        _, st = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, pn, return_status=True, precision=prec)
+        assert (st == -4).all(), prec
+    # T = 0 returns the initial grid
+    fm0 = nb.flowmap_grid_2D(fl, 0.0, 0.0, x, y, p)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    assert np.array_equal(fm0, np.stack([X, Y], -1))

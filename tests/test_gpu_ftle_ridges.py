@@ -1,0 +1,149 @@
+"""CUDA FTLE / Cauchy-Green / percentile / ridge kernels against the golden
+vectors and the CPU oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import apply_mask, reconstruct
+
+pytestmark = pytest.mark.gpu
+
+
+def test_ftle_golden(nb, golden, mask_dg):
+    fm = golden["fm"].astype(np.float64)
+    f = nb.ftle_grid_2D(fm, 8.0, 0.1, 0.1)
+    assert np.allclose(f.astype(np.float32), golden["ftle"])
+    fk = nb.ftle_grid_2D(fm, 8.0, 0.1, 0.1, mask=mask_dg)
+    assert np.allclose(fk.astype(np.float32), apply_mask(golden["ftle"], mask_dg))
+
+
+def test_C_eig_golden(nb, golden, mask_dg):
+    fm = golden["fm"].astype(np.float64)
+    ev, vec = nb.C_eig_2D(fm, 0.1, 0.1)
+    C_exp = reconstruct(golden["Cevals"], golden["Cevecs"])
+    assert np.allclose(reconstruct(ev.astype(np.float32), vec.astype(np.float32)), C_exp)
+    evm, vecm = nb.C_eig_2D(fm, 0.1, 0.1, mask_dg)
+    assert np.allclose(reconstruct(evm.astype(np.float32), vecm.astype(np.float32)),
+                       apply_mask(C_exp, mask_dg))
+    f = nb.ftle_from_eig(ev[..., 1], 8.0)
+    assert np.allclose(f.astype(np.float32), golden["ftle"])
+
+
+def _random_flowmap(nx, ny, seed=0):
+    rng = np.random.default_rng(seed)
+    X, Y = np.meshgrid(np.linspace(0, 2, nx), np.linspace(0, 1, ny), indexing="ij")
+    fm = np.stack([X + 0.05 * np.sin(7 * Y + 3 * X), Y + 0.05 * np.cos(5 * X)], -1)
+    return fm + 1e-3 * rng.standard_normal(fm.shape)
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (5, 7), (257, 129), (1000, 37)])
+def test_ftle_and_eig_parity(nb, orc, shape):
+    nx, ny = shape
+    fm = _random_flowmap(nx, ny)
+    dx, dy = 2.0 / (nx - 1), 1.0 / (ny - 1)
+    mask = np.random.default_rng(1).random((nx, ny)) < 0.1
+    for m in (None, mask):
+        f = nb.ftle_grid_2D(fm, -10.0, dx, dy, mask=m)
+        of = orc.ftle_grid_2D(fm, -10.0, dx, dy, mask=m)
+        # identical arithmetic up to the last bit of log()
+        np.testing.assert_allclose(f, of, rtol=5e-16, atol=0)
+        ev, vec = nb.C_eig_2D(fm, dx, dy, mask=m)
+        oev, ovec = orc.C_eig_2D(fm, dx, dy, mask=m)
+        assert np.array_equal(ev, oev) and np.array_equal(vec, ovec)
+        fe, ve = nb.ftle_evec_2D(fm, -10.0, dx, dy, mask=m)
+        np.testing.assert_allclose(fe, orc.ftle_from_eig(oev[..., 1], -10.0), rtol=5e-16, atol=0)
+        assert np.array_equal(ve, ovec[..., :, 1])
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 10, 1000, 169676, 1 << 20])
+@pytest.mark.parametrize("q", [0.0, 0.5, 37.5, 90.0, 99.99, 100.0])
+def test_percentile_bit_exact(nb, orc, n, q):
+    from numbacs_gb300 import _device as D
+    from numbacs_gb300 import _lib
+    rng = np.random.default_rng(n)
+    a = np.abs(rng.standard_normal(n))
+    a[: n // 4] = 0.0  # the zero border / non-stretching region of an FTLE field
+    if n > 10:
+        a[n // 2: n // 2 + 7] = a[n // 2]  # ties inside
+        a[-3:] = -a[-3:]
+    rng.shuffle(a)
+    t = torch.from_numpy(a).cuda()
+    L = _lib.load()
+    nbytes = L.nbcs_percentile_scratch_bytes(n)
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    _lib.check(L.nbcs_percentile(D.ptr(t), n, q, D.ptr(out), D.ptr(scratch), nbytes, D.stream_ptr()))
+    got = out.item()
+    exp = orc.percentile(a, q)
+    assert got == exp or (np.isnan(got) and np.isnan(exp)), (got, exp)
+
+
+def test_percentile_special_values(nb, orc):
+    from numbacs_gb300 import _device as D
+    from numbacs_gb300 import _lib
+    L = _lib.load()
+    cases = [np.array([1.0, np.nan, 3.0]), np.array([1.0, np.inf, 3.0]),
+             np.array([-np.inf, 2.0, 3.0, 4.0]), np.array([-0.0, 0.0, -0.0, 1.0]),
+             np.array([np.inf, -np.inf])]
+    for a in cases:
+        for q in (0.0, 50.0, 100.0):
+            t = torch.from_numpy(a).cuda()
+            sc = torch.empty(L.nbcs_percentile_scratch_bytes(len(a)), dtype=torch.uint8, device="cuda")
+            out = torch.empty(1, dtype=torch.float64, device="cuda")
+            _lib.check(L.nbcs_percentile(D.ptr(t), len(a), q, D.ptr(out), D.ptr(sc), sc.numel(),
+                                         D.stream_ptr()))
+            got, exp = out.item(), orc.percentile(a, q)
+            assert got == exp or (np.isnan(got) and np.isnan(exp)), (a, q, got, exp)
+
+
+def test_ridge_golden(nb, golden, coords_dg):
+    x, y = coords_dg
+    f = golden["ftle"].astype(np.float64)
+    e = golden["Cevecs"][:, :, :, 1].astype(np.float64)
+    rp = nb.ftle_ridge_pts(f, e, x, y)
+    assert rp.shape == golden["ridge_pts"].shape and np.allclose(rp, golden["ridge_pts"])
+    ridges = nb.ftle_ridges(f, e, x, y)
+    assert len(ridges) == int(golden["n_ridges"])
+    for k, r in enumerate(ridges):
+        assert np.allclose(r, golden["ridges_%d" % k])
+
+
+def _ridge_field(nx, ny, seed=0):
+    x, y = np.linspace(0, 2, nx), np.linspace(0, 1, ny)
+    fm = _random_flowmap(nx, ny, seed)
+    return x, y, fm
+
+
+@pytest.mark.parametrize("shape,pct,sdd", [((64, 32), 0, 0.0), ((676, 251), 90, 0.0),
+                                           ((301, 157), 50, 1e-3), ((2001, 7), 90, 0.0),
+                                           ((5, 5), 0, 0.0), ((4, 9), 90, 0.0)])
+def test_ridge_mask_bit_identical(nb, orc, shape, pct, sdd):
+    nx, ny = shape
+    x, y, fm = _ridge_field(nx, ny)
+    dx, dy = x[1] - x[0], y[1] - y[0]
+    # both sides get the SAME FTLE field and eigenvectors
+    oev, ovec = orc.C_eig_2D(fm, dx, dy)
+    f = orc.ftle_from_eig(oev[..., 1], 5.0)
+    e = np.ascontiguousarray(ovec[..., :, 1])
+    r_pts, rb, _, _ = nb.extraction._ftle_ridges(f, e, x, y, sdd, pct)
+    orp, orb, _ = orc._ridge_field(f, e, x, y, sdd, pct)
+    assert np.array_equal(rb, orb)
+    assert np.array_equal(r_pts, orp)
+    pts = nb.ftle_ridge_pts(f, e, x, y, sdd, pct)
+    assert np.array_equal(pts, orc.ftle_ridge_pts(f, e, x, y, sdd, pct))
+
+
+def test_ridge_compaction_large(nb):
+    # size-independent properties at a large size: count == mask sum, the
+    # compacted list is the row-major gather of the full array
+    nx, ny = 4001, 2001
+    x, y = torch.linspace(0, 2, nx, dtype=torch.float64, device="cuda"), torch.linspace(
+        0, 1, ny, dtype=torch.float64, device="cuda")
+    X, Y = torch.meshgrid(x, y, indexing="ij")
+    f = torch.sin(40 * X) * torch.cos(23 * Y) + 0.5 * torch.sin(9 * X * Y)
+    e = torch.stack([torch.cos(3 * Y), torch.sin(3 * Y)], -1).contiguous()
+    full, rb, _, _ = nb.extraction._ftle_ridges(f, e, x, y, 0.0, 90)
+    pts = nb.ftle_ridge_pts(f, e, x, y, 0.0, 90)
+    assert pts.shape[0] == int(rb.sum())
+    assert torch.equal(pts, full[rb.reshape(-1)])
+    assert pts.shape[0] > 1000
