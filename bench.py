@@ -1,0 +1,519 @@
+#!/usr/bin/env python3
+"""FTLE particles/s on the synthetic geophysical flow (one GB300).
+
+Workload (the benchmark configuration with a spline flow): divergence-free
+random velocity sampled on 121 (3-hourly) x 217 lon x 101 lat, tricubic spline,
+spherical coordinates; particles on a 0.2 deg grid (676 x 251 = 169,676),
+t0 = 180 h, T = -72 h; then the fused Cauchy-Green eigen/FTLE stencil and FTLE
+ridge extraction at the 90th percentile.  One step = flow map + FTLE/eigvec +
+ridge points for the whole grid.
+
+Precision: the headline path is the mixed-precision integrator at the loosest
+rtol (atol = 1e-2 rtol) whose flow map stays within 1e-6 of the domain extent
+of an FP64 solution converged to rtol 1e-12 (the FP64 plain path is measured
+the same way and reported beside it).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank integrates its own field (t0 + rank hours): weak
+scaling, no collective on the data path.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "FTLE particles/s at <=1e-6 flowmap err vs FP64; mixed/learned vs plain, same GPU"
+UNIT = "particles/s"
+L2_FLUSH_BYTES = 512 << 20  # > 126 MB L2
+RTOL_LADDER = [1e-6, 3e-7, 1e-7, 3e-8, 1e-8]
+
+# algorithmic work per attempted DOP853 step on a 2-D state (flops; an FMA
+# counts 2): stage combinations 264, update 48, error estimates 96, norms and
+# controller 30; plus 12 RHS evaluations.  Tricubic spherical RHS: 2 x 64
+# weighted taps (256) + weights/locate/conversion (~74) = 330 flops.
+FLOPS_STEP = 438
+FLOPS_RHS_SPLINE = 330
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--rtol", type=float, default=None, help="fixed rtol (skips the accuracy ladder)")
+    ap.add_argument("--quick", action="store_true",
+                    help="timed steps only (no ladder, plain comparison, e2e or CPU baseline)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ utils
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.lines = []
+        self.proc = None
+        self.index = index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_model():
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu part")):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# ------------------------------------------------------------- workload
+
+def geo_setup(t0):
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300 import workloads as W
+    t, lon, lat, U, V = W.geo_velocity(seed=0)
+    Ud, Vd = torch.from_numpy(U).cuda(), torch.from_numpy(V).cuda()
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, Ud, Vd)
+    flow = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    lonf, latf = W.geo_ftle_grid(0.2)
+    return dict(flow=flow, t=t, lon=lon, lat=lat, U=U, V=V, Cu=Cu.cpu().numpy(), Cv=Cv.cpu().numpy(),
+                grid=grid, lonf=lonf, latf=latf, t0=t0, T=W.GEO_T, pct=W.GEO_PERCENTILE,
+                params=np.array([-1.0]), dx=lonf[1] - lonf[0], dy=latf[1] - latf[0],
+                extent=lon[-1] - lon[0])
+
+
+def choose_rtol(nb, wl, x, y, precision, truth):
+    """Loosest rtol on the ladder whose flow map meets the accuracy bound.
+
+    The flow-map error of a run is |fm - fm_truth| per particle, fm_truth the
+    FP64 solution converged to rtol 1e-12; the bound asks the mean over the
+    grid to stay within 1e-6 of the domain extent (the maximum and the 99th /
+    99.9th percentiles are reported next to it: on this flow a handful of
+    trajectories that graze the clamped grid edge differ between any two valid
+    integrations by far more)."""
+    bound = 1e-6 * wl["extent"]
+    rows = []
+    chosen = None
+    for r in RTOL_LADDER:
+        fm = nb.flowmap_grid_2D(wl["flow"], wl["t0"], wl["T"], x, y, wl["params"], rtol=r,
+                                atol=1e-2 * r, precision=precision, return_status=True)[0]
+        err = (fm - truth).abs().amax(dim=-1).flatten()
+        q = torch_quantiles(err, [0.99, 0.999])
+        rows.append({"rtol": r, "mean_err": float(err.mean()), "q99_err": q[0], "q999_err": q[1],
+                     "max_err": float(err.max())})
+        if float(err.mean()) <= bound:
+            chosen = r
+            break
+    return chosen, rows
+
+
+def torch_quantiles(v, qs):
+    s = v.sort().values
+    n = s.numel()
+    return [float(s[min(n - 1, int(q * n))]) for q in qs]
+
+
+def run_ours(args, rank, world):
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300 import _device as D
+    from numbacs_gb300 import _lib
+
+    L = _lib.load()
+    wl = geo_setup(180.0 + rank)
+    x = torch.from_numpy(wl["lonf"]).cuda()
+    y = torch.from_numpy(wl["latf"]).cuda()
+    nx, ny = len(wl["lonf"]), len(wl["latf"])
+    npart = nx * ny
+    flow, t0, T, prm = wl["flow"], wl["t0"], wl["T"], wl["params"]
+
+    # precision / rtol selection against an FP64 truth
+    sel = {}
+    if args.rtol:
+        sel = {"mixed": {"rtol": args.rtol, "ladder": []}, "fp64": {"rtol": args.rtol, "ladder": []}}
+    else:
+        truth = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=1e-12, atol=1e-14,
+                                   return_status=True)[0]
+        for p_ in ("mixed", "fp64"):
+            r, rows = choose_rtol(nb, wl, x, y, p_, truth)
+            sel[p_] = {"rtol": r, "ladder": rows}
+        del truth
+    prec = args.precision
+    if prec == "auto":
+        prec = "mixed" if sel["mixed"]["rtol"] is not None else "fp64"
+    rtol = sel[prec]["rtol"] or RTOL_LADDER[-1]
+    atol = 1e-2 * rtol
+
+    # algorithmic step counts from the plain FP64 controller at this rtol
+    _, _, st64 = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol,
+                                    return_status=True, return_stats=True)
+    att = (st64[..., 0] + st64[..., 1]).to(torch.float64)
+    flops_launch = float((att * (FLOPS_STEP + 12 * FLOPS_RHS_SPLINE) + 2 * FLOPS_RHS_SPLINE).sum())
+    _, _, stp = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
+                                   return_status=True, return_stats=True)
+    nfcn_mean = float(stp[..., 2].double().mean())
+    rej_frac = float(stp[..., 1].sum()) / max(1.0, float((stp[..., 0] + stp[..., 1]).sum()))
+
+    fm_buf = torch.empty((nx, ny, 2), dtype=torch.float64, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        fm = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
+                                out=fm_buf, return_status=True)[0]
+        if ev is not None:
+            ev[1].record(stream)
+        f, e = nb.ftle_evec_2D(fm, T, wl["dx"], wl["dy"])
+        if ev is not None:
+            ev[2].record(stream)
+        pts = nb.ftle_ridge_pts(f, e, x, y, 0.0, wl["pct"])
+        if ev is not None:
+            ev[3].record(stream)
+        return pts
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = L.nbcs_launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()  # cold L2 for every step (outside the timed events)
+        step(evs[k])
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = L.nbcs_launch_count() - launches0
+    ck = clocks.stop()
+    t_step = [e[0].elapsed_time(e[3]) for e in evs]
+    t_fm = [e[0].elapsed_time(e[1]) for e in evs]
+    t_ftle = [e[1].elapsed_time(e[2]) for e in evs]
+    t_ridge = [e[2].elapsed_time(e[3]) for e in evs]
+    ms = sum(t_step) / len(t_step)
+    ms = max_over_ranks(ms, world)
+    value = world * npart / (ms * 1e-3)
+
+    # plain FP64 path, same step, for the mixed-vs-plain ratio
+    t_plain = None
+    if prec == "mixed" and sel["fp64"]["rtol"] is not None and not args.quick:
+        rp = sel["fp64"]["rtol"]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(2):
+            nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rp, atol=1e-2 * rp, out=fm_buf,
+                               return_status=True)
+        ts = []
+        for _ in range(3):
+            flush.zero_()
+            e0.record(stream)
+            fm = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rp, atol=1e-2 * rp, out=fm_buf,
+                                    return_status=True)[0]
+            f, e = nb.ftle_evec_2D(fm, T, wl["dx"], wl["dy"])
+            nb.ftle_ridge_pts(f, e, x, y, 0.0, wl["pct"])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        t_plain = sum(ts) / len(ts)
+
+    # FP32 / FP64 FMA peak probes (burst) for the compute roofline
+    sink = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+
+    def probe(p):
+        import ctypes
+        fl = ctypes.c_double(0.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = 0.0
+        for _ in range(3):
+            a.record(stream)
+            _lib.check(L.nbcs_probe_fma(p, 4096, D.ptr(sink), ctypes.byref(fl), D.stream_ptr()))
+            b.record(stream)
+            torch.cuda.synchronize()
+            best = max(best, fl.value / (a.elapsed_time(b) * 1e-3) / 1e12)
+        return best
+
+    peak32 = probe(_lib.PREC_MIXED)
+    peak64 = probe(_lib.PREC_FP64)
+    fm_ms = sum(t_fm) / len(t_fm)
+    achieved = flops_launch / (fm_ms * 1e-3) / 1e12
+    peak = peak32 if prec == "mixed" else peak64
+    traffic = _profile_traffic(prec)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if prec == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": "geo spline flow 121x217x101, 676x251 particles, t0=180h T=-72h, "
+                               "FTLE + ridges p90", "particles": npart, "precision": prec,
+                   "rtol": rtol, "atol": atol, "l2": "flushed between timed steps",
+                   "parallelism": "field per GPU" if world > 1 else "single GPU"},
+        "gpu_launches": int(launches),
+        "clocks": ck,
+        "roofline": {"bound": "fp32" if prec == "mixed" else "fp64", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "traffic": traffic,
+                     "peak_source": "in-run FMA probe (nbcs_probe_fma), burst",
+                     "kernel": "flowmap32_kernel" if prec == "mixed" else "flowmap64_kernel",
+                     "flops_per_launch": flops_launch, "launch_ms": fm_ms},
+        "breakdown_ms": {"flowmap": fm_ms, "ftle_evec": sum(t_ftle) / len(t_ftle),
+                         "ridge": sum(t_ridge) / len(t_ridge)},
+        "accuracy": {"bound": 1e-6 * wl["extent"], "mixed": sel["mixed"], "fp64": sel["fp64"]},
+        "integrator": {"rhs_evals_per_particle": nfcn_mean, "rejected_fraction": rej_frac,
+                       "attempted_steps_fp64": float(att.mean())},
+        "plain_fp64": ({"ms_per_step": t_plain, "value": world * npart / (t_plain * 1e-3),
+                        "rtol": sel["fp64"]["rtol"], "speedup_mixed_over_plain": t_plain / ms}
+                       if t_plain else None),
+    }
+    if not args.no_e2e and not args.quick:
+        out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
+    if not args.no_cpu_baseline and not args.quick and rank == 0:
+        out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value)
+    return out
+
+
+def _profile_traffic(prec):
+    """DRAM bytes per launch of the integrator from the committed ncu summary."""
+    name = "flowmap32_geo.md" if prec == "mixed" else "flowmap64_geo.md"
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_e2e(nb, D, wl, prec, rtol, atol, args, world):
+    """Same step through the public numpy API: host arrays in, host results out."""
+    import torch
+    lonf, latf = wl["lonf"], wl["latf"]
+
+    def step():
+        fm = nb.flowmap_grid_2D(wl["flow"], wl["t0"], wl["T"], lonf, latf, wl["params"], rtol=rtol,
+                                atol=atol, precision=prec, return_status=True)[0]
+        f, e = nb.ftle_evec_2D(fm, wl["T"], wl["dx"], wl["dy"])
+        return nb.ftle_ridge_pts(f, e, lonf, latf, 0.0, wl["pct"])
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    h0, d0 = D.transfer_bytes["h2d"], D.transfer_bytes["d2h"]
+    K = max(3, args.steps)
+    barrier(world)
+    t = time.perf_counter()
+    for _ in range(K):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    dt = (time.perf_counter() - t) / K
+    dt = max_over_ranks(dt, world)
+    npart = len(lonf) * len(latf)
+    return {"value": world * npart / dt, "unit": UNIT,
+            "h2d_bytes_per_step": (D.transfer_bytes["h2d"] - h0) // K,
+            "d2h_bytes_per_step": (D.transfer_bytes["d2h"] - d0) // K,
+            "ms_per_step": dt * 1e3, "api": "numpy in / numpy out (pageable host memory)"}
+
+
+def cpu_sample_rate(wl, rtol, atol, budget_s, threads):
+    """Oracle particles/s on the host cores over a bounded sample of the grid.
+
+    Integrates every `stride`-th longitude row (all latitudes) with the oracle's
+    DOP853 + spline RHS, then adds the per-particle cost of the oracle's
+    FTLE / eigen / ridge stencils measured on the full field."""
+    import oracle
+    oracle.build()
+    of = oracle.spline_flow(wl["grid"], wl["Cu"], wl["Cv"], spherical=1)
+    lonf, latf = wl["lonf"], wl["latf"]
+    nx = len(lonf)
+    # calibrate on a few rows, then size the sample to the budget
+    rows = lonf[:: max(1, nx // 8)][:4]
+    t = time.perf_counter()
+    oracle.flowmap_grid_2D(of, wl["t0"], wl["T"], rows, latf, wl["params"], rtol=rtol, atol=atol,
+                           nthreads=threads)
+    per_row = (time.perf_counter() - t) / len(rows)
+    nrows = int(min(nx, max(4, budget_s / max(per_row, 1e-6))))
+    stride = max(1, nx // nrows)
+    sample = lonf[::stride]
+    t = time.perf_counter()
+    fm = oracle.flowmap_grid_2D(of, wl["t0"], wl["T"], sample, latf, wl["params"], rtol=rtol,
+                                atol=atol, nthreads=threads)
+    t_fm = time.perf_counter() - t
+    n_sample = len(sample) * len(latf)
+    # stencil stages on a full-size field (cheap): reuse the sample rows tiled
+    full = np.resize(fm, (nx, len(latf), 2))
+    t = time.perf_counter()
+    ev, vec = oracle.C_eig_2D(full, wl["dx"], wl["dy"])
+    f = oracle.ftle_from_eig(ev[..., 1], wl["T"])
+    oracle.ftle_ridge_pts(f, np.ascontiguousarray(vec[..., :, 1]), lonf, latf, 0.0, wl["pct"])
+    t_st = time.perf_counter() - t
+    per_particle = t_fm / n_sample + t_st / (nx * len(latf))
+    return 1.0 / per_particle, n_sample, stride, t_fm + t_st
+
+
+def run_cpu_baseline(wl, rtol, atol, budget_s, value_gpu=None):
+    threads = os.cpu_count() or 1
+    rate, n, stride, secs = cpu_sample_rate(wl, rtol, atol, budget_s, threads)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d particles (every %d-th lon row x all 251 lat) integrated by the C "
+                      "oracle (DOP853 + tricubic spline, OpenMP) + full-field FTLE/eig/ridge "
+                      "stencils; %.1f s of CPU work; %s" % (n, stride, secs, cpu_model()),
+            "rtol": rtol}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores: numba/numbalsoda are not
+    installable here, so the C restatement of the same algorithms (oracle) is
+    timed, all host threads, a bounded sample of the workload per step."""
+    import torch
+    from numbacs_gb300 import workloads as W
+    t, lon, lat, U, V = W.geo_velocity(seed=0, device="cpu")
+    import oracle
+    oracle.build()
+    grid, Cu, Cv = oracle.get_interp_arrays_2D(t, lon, lat, U, V)
+    lonf, latf = W.geo_ftle_grid(0.2)
+    wl = dict(grid=grid, Cu=Cu, Cv=Cv, lonf=lonf, latf=latf, t0=180.0, T=W.GEO_T,
+              pct=W.GEO_PERCENTILE, params=np.array([-1.0]), dx=lonf[1] - lonf[0],
+              dy=latf[1] - latf[0])
+    rtol, atol = 1e-6, 1e-8
+    budget = max(2.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sample_rate(wl, rtol, atol, budget, os.cpu_count())
+    rates, secs = [], 0.0
+    n = stride = 0
+    for _ in range(args.steps):
+        r, n, stride, s = cpu_sample_rate(wl, rtol, atol, budget, os.cpu_count())
+        rates.append(r)
+        secs += s
+    value = statistics.median(rates)
+    cores = os.cpu_count()
+    sample = ("%d particles (every %d-th lon row) per step, C restatement of the reference's "
+              "numba path (numba/numbalsoda/interpolation not installable), %s" % (n, stride, cpu_model()))
+    del torch
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * 169676 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "geo spline flow 121x217x101, 676x251 particles, t0=180h T=-72h, "
+                                   "FTLE + ridges p90", "rtol": rtol, "atol": atol},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, 0, int(os.environ.get("WORLD_SIZE", "1")))))
+        return 0
+    rank, world, _ = dist_setup()
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -61,15 +61,19 @@ typedef struct nbcs_flow {
     double r;          /* SPLINE2D spherical: radius (km) for km/h -> deg/h */
     double grid[9];    /* SPLINE2D: t0,t1,nt, x0,x1,nx, y0,y1,ny (UCGrid tuple) */
     const double* coef_uv;  /* SPLINE2D FP64 coefficients (device), required */
-    const float* coef_uv32; /* SPLINE2D FP32 copy (device), required for NBCS_PREC_MIXED */
+    /* SPLINE2D FP32 copy (device), required for NBCS_PREC_MIXED, in the "pair"
+     * layout: entry k (16 bytes) holds u_k, v_k, u_{k+1}, v_{k+1}; n entries. */
+    const float* coef_uv32;
 } nbcs_flow;
 
 /* integrator options; a NULL opts pointer means all defaults */
 typedef struct nbcs_opts {
     int32_t precision;     /* NBCS_PREC_* (default FP64) */
     int32_t max_steps;     /* attempted-step limit per particle (default 100000) */
-    int32_t threads_per_block; /* 0 = library default */
-    int32_t blocks_per_sm;     /* 0 = library default */
+    int32_t threads_per_block; /* FP64 path: 0 = library default (128) */
+    int32_t blocks_per_sm;     /* grid cap in blocks per SM; 0 = one block per particle tile */
+    int32_t lanes_per_particle; /* mixed spline path: 1, 2 or 4 lanes share a particle; 0 = auto */
+    int32_t reserved;
     int32_t* stats;        /* optional device (n,3) int32: accepted, rejected, RHS evals */
     const void* step_model; /* optional learned initial-step model (device), see nbcs_mlp_* */
 } nbcs_opts;
@@ -89,7 +93,7 @@ int nbcs_spline_prefilter_3d(const double* f, int32_t nt, int32_t nx, int32_t ny
 
 /* get_flow_2D coefficient capture (flows.py:156-254 closes over C_eval_u /
  * C_eval_v): interleave cu, cv (n nodes each) into coef_uv (2n doubles) and,
- * if coef_uv32 != NULL, an FP32 copy (2n floats). */
+ * if coef_uv32 != NULL, an FP32 copy in the pair layout (4n floats). */
 int nbcs_spline_pack_uv(const double* cu, const double* cv, int64_t n, double* coef_uv,
                         float* coef_uv32, void* stream);
 
@@ -153,6 +157,18 @@ int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int
                    const double* y, int32_t ny, double sdd_thresh, double percentile,
                    uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
                    void* scratch, size_t scratch_bytes, void* stream);
+
+/* ------------------------------------------------------------ measurement */
+/* No counterpart in the reference (which has no GPU path). */
+
+/* Number of kernels this library has launched in the process so far. */
+unsigned long long nbcs_launch_count(void);
+
+/* FMA throughput probe for the compute roofline: one launch of 8*SMs blocks
+ * of 256 threads, 8 FMA chains each, `iters` iterations, in FP64 (precision
+ * NBCS_PREC_FP64) or FP32.  `sink` is a device buffer of >= 64 KiB; *flops
+ * (host) receives the flop count of the launch (an FMA counts 2). */
+int nbcs_probe_fma(int32_t precision, int64_t iters, void* sink, double* flops, void* stream);
 
 #ifdef __cplusplus
 }

@@ -10,6 +10,9 @@ import torch
 
 from . import _lib
 
+# bytes moved between host and device by the numpy-in / numpy-out paths
+transfer_bytes = {"h2d": 0, "d2h": 0}
+
 
 def require_cuda():
     if not torch.cuda.is_available():
@@ -46,6 +49,7 @@ def to_dev(a, dtype=torch.float64):
             t = t.to(dtype)
         return t.contiguous()
     arr = np.ascontiguousarray(np.asarray(a), dtype=_np_dtype(dtype))
+    transfer_bytes["h2d"] += arr.nbytes
     return torch.from_numpy(arr).to(device(), non_blocking=False)
 
 
@@ -74,4 +78,5 @@ def finish(t, as_torch):
     """Return a device tensor as-is (torch callers) or as a numpy array."""
     if as_torch:
         return t
+    transfer_bytes["d2h"] += t.numel() * t.element_size()
     return t.cpu().numpy()

@@ -30,6 +30,7 @@ class NbcsOpts(ctypes.Structure):
     """Mirror of ``struct nbcs_opts``."""
     _fields_ = [("precision", ctypes.c_int32), ("max_steps", ctypes.c_int32),
                 ("threads_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("lanes_per_particle", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("stats", ctypes.c_void_p), ("step_model", ctypes.c_void_p)]
 
 
@@ -54,6 +55,8 @@ SIGNATURES = {
     "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
                                       _vp, _sz, _vp]),
+    "nbcs_launch_count": (ctypes.c_ulonglong, []),
+    "nbcs_probe_fma": (ctypes.c_int, [_i32, _i64, _vp, ctypes.POINTER(ctypes.c_double), _vp]),
 }
 
 _lib = None

@@ -33,6 +33,7 @@ SOURCES = [
     ("ftle.cu", ["-fmad=false"]),
     ("spline.cu", ["-fmad=false"]),
     ("ridges.cu", ["-fmad=false"]),
+    ("probe.cu", []),
 ]
 
 

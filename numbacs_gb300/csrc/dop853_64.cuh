@@ -9,6 +9,7 @@
 // entries; compiled with -fmad=false so results match the CPU oracle.
 #pragma once
 
+#include "detmath.h"
 #include "dop853_tableau.h"
 #include "nbcs_internal.cuh"
 
@@ -55,7 +56,7 @@ __device__ __forceinline__ double dop853_hinit64(const Flow& fl, const Params& P
     der2 = sqrt(der2) / h;
     der12 = dmax_(fabs(der2), sqrt(dnf));
     if (der12 <= 1.0e-15) h1 = dmax_(1.0e-6, fabs(h) * 1.0e-3);
-    else h1 = pow(0.01 / der12, 1.0 / 8.0);
+    else h1 = nbcs_root8(0.01 / der12);
     h = dmin_(100.0 * fabs(h), dmin_(h1, hmax));
     return posneg >= 0.0 ? fabs(h) : -fabs(h);
 }
@@ -66,7 +67,6 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
                               double rtol, double atol, int nmax, Dop853Stats* st)
 {
     const double uround = 2.3e-16, safe = 0.9, facc1 = 1.0 / 0.333, facc2 = 1.0 / 6.0;
-    const double expo1 = 1.0 / 8.0;
     double k1[2], k2[2], k3[2], k4[2], k5[2], k6[2], k7[2], k8[2], k9[2], k10[2], yy1[2];
     double facold = 1.0e-4;
     double posneg = (xend - x) >= 0.0 ? 1.0 : -1.0;
@@ -167,7 +167,7 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
         if (deno <= 0.0) deno = 1.0;
         err = fabs(h) * err * sqrt(1.0 / (deno * 2.0));
         if (isnan(err)) { status = NBCS_PARTICLE_NONFINITE; break; }
-        fac11 = pow(err, expo1);
+        fac11 = nbcs_root8(err);  // err^(1/8)
         fac = fac11;  // beta = 0: the Lund stabilisation factor facold^beta is 1
         fac = dmax_(facc2, dmin_(facc1, fac / safe));
         hnew = h / fac;

@@ -167,6 +167,7 @@ extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, 
     a.nmax = o.max_steps;
     a.threads = o.threads_per_block;
     a.blocks_per_sm = o.blocks_per_sm;
+    a.lanes = o.lanes_per_particle;
     a.step_model = o.step_model;
     a.stream = as_stream(stream);
     if (o.precision == NBCS_PREC_MIXED) return launch_flowmap32(flow, a);

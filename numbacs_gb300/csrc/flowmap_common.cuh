@@ -17,7 +17,7 @@ struct FlowmapArgs {
     int32_t* stats;
     double rtol, atol;
     int nmax;
-    int threads, blocks_per_sm;
+    int threads, blocks_per_sm, lanes;
     const void* step_model;
     cudaStream_t stream;
 };

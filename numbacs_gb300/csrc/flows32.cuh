@@ -1,9 +1,23 @@
 // FP32 device right-hand sides for the mixed-precision integrator.
 //
 // Same fields as flows64.cuh (double gyre flows.py:1146-1158, Bickley jet
-// flows.py:1182-1213, tricubic spline flows.py:154-254) rewritten for the FP32
-// pipe: sincospif instead of sin(pi*x), one expf for tanh/sech^2, FMA-friendly
-// B-spline weights, FP32 coefficients interleaved (u, v) per node.
+// flows.py:1182-1213, tricubic spline flows.py:154-254) evaluated on the FP32
+// pipe.  Positions and times arrive as unevaluated pairs (hi, s) -- the
+// particle's compensated coordinate plus the stage increment -- so that the
+// spline can form its cell-local offsets to FP32 *relative* accuracy: an
+// absolute coordinate rounded to one float (lon ~ 100 deg, t ~ 150 h) would
+// carry ~4e-6 of absolute error into every velocity sample.
+//
+// The double gyre is written as sin(pi f) = -sinpi(w), w = f - 1 =
+// a x (x - 2) + (x - 1), which is exactly +-1 on the invariant walls x = 0 and
+// x = 2 (FP32 rounding of f = a x^2 + (1 - 2a) x would push wall particles into
+// the unstable direction).
+//
+// The spline RHS can be evaluated cooperatively by a group of LP = 1, 2 or 4
+// adjacent lanes that hold the same particle: lane q of the group sums the
+// time levels q, q + LP, ... of the 4x4x4 stencil and a butterfly of
+// __shfl_xor_sync adds the partial sums, so every lane of the group ends with
+// bit-identical velocities (float addition is commutative).
 #pragma once
 
 #include "nbcs_internal.cuh"
@@ -15,66 +29,104 @@ struct ParamsF {
 };
 
 struct FlowDG32 {
-    __device__ __forceinline__ void operator()(float t, const float* y, float* dy,
-                                               const ParamsF& P) const
+    static constexpr int LP = 1;
+    __device__ __forceinline__ void operator()(float th, float ts, const float* yh, const float* ys,
+                                               float* dy, const ParamsF& P) const
     {
         const float* p = P.v;
-        float tt = p[0] * t;
+        float tt = p[0] * (th + ts);
+        float x = yh[0] + ys[0], y = yh[1] + ys[1];
         float a = p[2] * sinf(fmaf(p[4], tt, p[5]));
         float b = fmaf(-2.0f, a, 1.0f);
-        float x0 = y[0];
-        float f = fmaf(a, x0, b) * x0;
-        float df = fmaf(2.0f * a, x0, b);
-        float sf, cf, sy, cy;
-        sincospif(f, &sf, &cf);
-        sincospif(y[1], &sy, &cy);
+        float w = fmaf(a * x, x - 2.0f, x - 1.0f);  // f - 1
+        float df = fmaf(2.0f * a, x, b);
+        float sw, cw, sy, cy;
+        sincospif(w, &sw, &cw);  // sin(pi f) = -sw, cos(pi f) = -cw
+        sincospif(y, &sy, &cy);
         const float piA = 3.14159265358979f * p[1];
-        dy[0] = p[0] * fmaf(-piA * sf, cy, -p[3] * x0);
-        dy[1] = p[0] * fmaf(piA * cf * sy, df, -p[3] * y[1]);
+        dy[0] = p[0] * fmaf(piA * sw, cy, -p[3] * x);
+        dy[1] = p[0] * fmaf(-piA * cw * sy, df, -p[3] * y);
     }
 };
 
 struct FlowBickley32 {
-    __device__ __forceinline__ void operator()(float t, const float* y, float* dy,
-                                               const ParamsF& P) const
+    static constexpr int LP = 1;
+    __device__ __forceinline__ void operator()(float th, float ts, const float* yh, const float* ys,
+                                               float* dy, const ParamsF& P) const
     {
         const float* p = P.v;
-        float tt = p[0] * t;
-        float Y = y[1] / p[2];
+        float tt = p[0] * (th + ts);
+        float x = yh[0] + ys[0], y = yh[1] + ys[1];
+        float Y = y / p[2];
         // tanh(Y) and sech^2(Y) from e = exp(-2|Y|): tanh = (1-e)/(1+e), sech^2 = 4e/(1+e)^2
         float e = __expf(-2.0f * fabsf(Y));
         float inv = 1.0f / (1.0f + e);
-        float th = copysignf((1.0f - e) * inv, Y);
+        float th_ = copysignf((1.0f - e) * inv, Y);
         float sech2 = 4.0f * e * inv * inv;
         float sn1, cs1, sn2, cs2, sn3, cs3;
-        sincosf(p[6] * fmaf(-p[9], tt, y[0]), &sn1, &cs1);
-        sincosf(p[7] * fmaf(-p[10], tt, y[0]), &sn2, &cs2);
-        sincosf(p[8] * fmaf(-p[11], tt, y[0]), &sn3, &cs3);
+        sincosf(p[6] * fmaf(-p[9], tt, x), &sn1, &cs1);
+        sincosf(p[7] * fmaf(-p[10], tt, x), &sn2, &cs2);
+        sincosf(p[8] * fmaf(-p[11], tt, x), &sn3, &cs3);
         float cs = fmaf(p[3], cs1, fmaf(p[4], cs2, p[5] * cs3));
         float sn = fmaf(p[3] * p[6], sn1, fmaf(p[4] * p[7], sn2, p[5] * p[8] * sn3));
-        dy[0] = p[0] * (p[1] * sech2 * fmaf(2.0f * th, cs, 1.0f));
+        dy[0] = p[0] * (p[1] * sech2 * fmaf(2.0f * th_, cs, 1.0f));
         dy[1] = -p[0] * (p[1] * p[2] * sech2 * sn);
     }
 };
 
+// One spline axis: node k sits at a + k*d, with a and d kept as float pairs
+// (hi + lo) so node positions can be rebuilt to ~2^-48 relative accuracy.
+struct AxisF {
+    float a_h, a_l, d_h, d_l, dinv;
+    int n;
+};
+
 struct SplineGridF {
-    float a[3], b[3], dinv[3];
-    int n[3];
-    int sx, st;
+    AxisF ax[3];  // t, x, y
+    int sx, st;   // node strides of the (nt+2, nx+2, ny+2) coefficient block
 };
 
 inline SplineGridF make_grid_f(const double* g)
 {
     SplineGridF s;
     for (int d = 0; d < 3; ++d) {
-        s.a[d] = (float)g[3 * d];
-        s.b[d] = (float)g[3 * d + 1];
-        s.n[d] = (int)g[3 * d + 2];
-        s.dinv[d] = (float)((double)(s.n[d] - 1) / (g[3 * d + 1] - g[3 * d]));
+        double a = g[3 * d], b = g[3 * d + 1];
+        int n = (int)g[3 * d + 2];
+        double dd = (b - a) / (double)(n - 1);
+        AxisF& A = s.ax[d];
+        A.a_h = (float)a;
+        A.a_l = (float)(a - (double)A.a_h);
+        A.d_h = (float)dd;
+        A.d_l = (float)(dd - (double)A.d_h);
+        A.dinv = (float)((double)(n - 1) / (b - a));
+        A.n = n;
     }
-    s.sx = s.n[2] + 2;
-    s.st = (s.n[1] + 2) * (s.n[2] + 2);
+    s.sx = s.ax[2].n + 2;
+    s.st = (s.ax[1].n + 2) * (s.ax[2].n + 2);
     return s;
+}
+
+// Cell index and offset t in [0, 1] of the coordinate vh + vs on one axis.
+// extrap_mode "constant": coordinates outside [a, b] are clamped to the ends.
+__device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, float* t)
+{
+    float u = ((vh + vs) - A.a_h) * A.dinv;
+    if (u != u) { *t = u; return 0; }  // NaN propagates
+    if (!(u > 0.0f)) { *t = 0.0f; return 0; }
+    if (u >= (float)(A.n - 1)) { *t = 1.0f; return A.n - 2; }
+    int i = min((int)u, A.n - 2);
+    float fi = (float)i;
+    // node position a + i*d as s + lo (exact product, two-sum on the hi parts)
+    float p = __fmul_rn(fi, A.d_h);
+    float e = fmaf(fi, A.d_h, -p);
+    e = fmaf(fi, A.d_l, e);
+    float s = __fadd_rn(A.a_h, p);
+    float bb = __fsub_rn(s, A.a_h);
+    float err = __fadd_rn(__fsub_rn(A.a_h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    float lo = err + (e + A.a_l);
+    float r = __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
+    *t = r * A.dinv;
+    return i;
 }
 
 __device__ __forceinline__ void bspline_w32(float t, float* w)
@@ -88,77 +140,95 @@ __device__ __forceinline__ void bspline_w32(float t, float* w)
     w[3] = s * t2 * t;
 }
 
-__device__ __forceinline__ int spline_locate32(const SplineGridF& g, int d, float x, float* t)
+// B-spline weight of time level a in {0..3} at offset t (one basis function)
+__device__ __forceinline__ float bspline_w32_one(float t, int a)
 {
-    x = fminf(fmaxf(x, g.a[d]), g.b[d]);  // extrap_mode "constant"
-    float u = (x - g.a[d]) * g.dinv[d];
-    int i = (int)floorf(u);
-    i = max(0, min(i, g.n[d] - 2));
-    *t = u - (float)i;
-    return i;
+    const float s = 1.0f / 6.0f;
+    float t2 = t * t, u = 1.0f - t;
+    switch (a) {
+    case 0: return s * u * u * u;
+    case 1: return s * fmaf(fmaf(3.0f, t, -6.0f), t2, 4.0f);
+    case 2: return s * fmaf(fmaf(fmaf(-3.0f, t, 3.0f), t, 3.0f), t, 1.0f);
+    default: return s * t2 * t;
+    }
 }
 
-__device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float2* __restrict__ c,
-                                                 float t, float x, float y, float* u, float* v)
+// Group-cooperative tricubic evaluation.  Coefficients use the "pair" layout:
+// entry k holds (u_k, v_k, u_{k+1}, v_{k+1}) as one float4, so the 4 y taps of
+// a stencil row are two aligned 16-byte loads.
+template <int LP>
+__device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float4* __restrict__ c,
+                                                 int it, int ix, int iy, float ft, const float* wx,
+                                                 const float* wy, float* u, float* v)
 {
-    float ft, fx, fy, wt[4], wx[4], wy[4];
-    int it = spline_locate32(g, 0, t, &ft);
-    int ix = spline_locate32(g, 1, x, &fx);
-    int iy = spline_locate32(g, 2, y, &fy);
-    bspline_w32(ft, wt);
-    bspline_w32(fx, wx);
-    bspline_w32(fy, wy);
-    const float2* base = c + (size_t)it * g.st + (size_t)ix * g.sx + iy;
+    const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
     float au = 0.0f, av = 0.0f;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
+    for (int r = 0; r < 4 / LP; ++r) {
+        const int a = q + r * LP;
+        const float wt = bspline_w32_one(ft, a);
+        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy;
         float su = 0.0f, sv = 0.0f;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float2* row = base + (size_t)a * g.st + (size_t)b * g.sx;
-            float2 r0 = __ldg(row), r1 = __ldg(row + 1), r2 = __ldg(row + 2), r3 = __ldg(row + 3);
-            float bu = fmaf(wy[0], r0.x, fmaf(wy[1], r1.x, fmaf(wy[2], r2.x, wy[3] * r3.x)));
-            float bv = fmaf(wy[0], r0.y, fmaf(wy[1], r1.y, fmaf(wy[2], r2.y, wy[3] * r3.y)));
+            const float4* row = base + (size_t)b * g.sx;
+            float4 p0 = __ldg(row), p1 = __ldg(row + 2);
+            float bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
+            float bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
             su = fmaf(wx[b], bu, su);
             sv = fmaf(wx[b], bv, sv);
         }
-        au = fmaf(wt[a], su, au);
-        av = fmaf(wt[a], sv, av);
+        au = fmaf(wt, su, au);
+        av = fmaf(wt, sv, av);
+    }
+    if (LP > 1) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned gmask = ((1u << LP) - 1u) << (lane & ~(unsigned)(LP - 1));
+#pragma unroll
+        for (int o = 1; o < LP; o <<= 1) {
+            au += __shfl_xor_sync(gmask, au, o);
+            av += __shfl_xor_sync(gmask, av, o);
+        }
     }
     *u = au;
     *v = av;
 }
 
-// Python float modulo in FP32.
-__device__ __forceinline__ float py_fmodf(float a, float b)
-{
-    float m = fmodf(a, b);
-    if (m != 0.0f && ((b < 0.0f) != (m < 0.0f))) m += b;
-    return m;
-}
-
-template <int SPH>
+template <int SPH, int LP_>
 struct FlowSpline32 {
+    static constexpr int LP = LP_;
     SplineGridF g;
-    const float2* __restrict__ c;
+    const float4* __restrict__ c;
     float deg_per_km;  // 180 / (pi r)
 
-    __device__ __forceinline__ void operator()(float t, const float* y, float* dy,
-                                               const ParamsF& P) const
+    __device__ __forceinline__ void operator()(float th, float ts, const float* yh, const float* ys,
+                                               float* dy, const ParamsF& P) const
     {
         const float* p = P.v;
-        float tt = p[0] * t;
-        float u, v;
+        const float p0 = p[0];
+        float xh = yh[0];
         if (SPH == 1 || SPH == 2) {
-            float xx = SPH == 1 ? py_fmodf(y[0] - 180.0f, 360.0f) - 180.0f : py_fmodf(y[0], 360.0f);
-            float yy = y[1];
-            spline_eval_uv32(g, c, tt, xx, yy, &u, &v);
-            dy[0] = p[0] * u * deg_per_km / cospif(yy * (1.0f / 180.0f));
-            dy[1] = p[0] * v * deg_per_km;
+            // lon wrap: ((x - 180) % 360) - 180 = x - 360 floor((x + 180) / 360)   (SPH 1)
+            //           x % 360               = x - 360 floor(x / 360)             (SPH 2)
+            float xv = yh[0] + ys[0];
+            float k = floorf((SPH == 1 ? xv + 180.0f : xv) * (1.0f / 360.0f));
+            if (k != 0.0f) xh = fmaf(-360.0f, k, xh);
+        }
+        float ft, fx, fy, wx[4], wy[4];
+        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft);
+        int ix = locate_pair(g.ax[1], xh, ys[0], &fx);
+        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy);
+        bspline_w32(fx, wx);
+        bspline_w32(fy, wy);
+        float u, v;
+        spline_eval_uv32<LP>(g, c, it, ix, iy, ft, wx, wy, &u, &v);
+        if (SPH == 1 || SPH == 2) {
+            float lat = yh[1] + ys[1];
+            dy[0] = p0 * u * deg_per_km / cospif(lat * (1.0f / 180.0f));
+            dy[1] = p0 * v * deg_per_km;
         } else {
-            spline_eval_uv32(g, c, tt, y[0], y[1], &u, &v);
-            dy[0] = p[0] * u;
-            dy[1] = p[0] * v;
+            dy[0] = p0 * u;
+            dy[1] = p0 * v;
         }
     }
 };

@@ -11,6 +11,7 @@
 //   spline RHS    flows.py:154-254 (interpolation.eval_spline, k=3)
 #pragma once
 
+#include "detmath.h"
 #include "nbcs_internal.cuh"
 
 namespace nbcs {
@@ -145,7 +146,7 @@ struct FlowSpline64 {
             double xx = SPH == 1 ? py_fmod(y[0] - 180.0, 360.0) - 180.0 : py_fmod(y[0], 360.0);
             double yy = y[1];
             spline_eval_uv64(g, c, extrap, tt, xx, yy, &u, &v);
-            dy[0] = p[0] * u * 180.0 / (NBCS_PI * r * cos(yy * NBCS_PI / 180.0));
+            dy[0] = p[0] * u * 180.0 / (NBCS_PI * r * nbcs_cos_deg(yy));
             dy[1] = p[0] * v * 180.0 / (NBCS_PI * r);
         } else {
             spline_eval_uv64(g, c, extrap, tt, y[0], y[1], &u, &v);

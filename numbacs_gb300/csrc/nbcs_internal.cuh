@@ -19,7 +19,13 @@ int set_error(int code, const char* fmt, ...);
                                      cudaGetErrorString(e_), __FILE__, __LINE__);  \
     } while (0)
 
-#define NBCS_LAUNCH_CHECK() NBCS_CUDA_TRY(cudaGetLastError())
+// Count one kernel launch (nbcs_launch_count) and surface launch errors.
+void count_launch();
+#define NBCS_LAUNCH_CHECK()                  \
+    do {                                     \
+        ::nbcs::count_launch();              \
+        NBCS_CUDA_TRY(cudaGetLastError());   \
+    } while (0)
 
 // Number of SMs of the current device (cached per device).
 int sm_count();

@@ -75,14 +75,23 @@ __global__ void prefilter_lines_kernel(const double* __restrict__ f, double* __r
     }
 }
 
+// FP64 (u, v) per node, and the FP32 "pair" layout: entry k = (u_k, v_k,
+// u_{k+1}, v_{k+1}) so a 4-tap stencil row is two aligned 16-byte loads.
 __global__ void pack_uv_kernel(const double* __restrict__ cu, const double* __restrict__ cv, long n,
-                               double2* __restrict__ uv, float2* __restrict__ uv32)
+                               double2* __restrict__ uv, float4* __restrict__ uv32)
 {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += (long)gridDim.x * blockDim.x) {
         double u = cu[k], v = cv[k];
         uv[k] = make_double2(u, v);
-        if (uv32) uv32[k] = make_float2((float)u, (float)v);
+        if (uv32) {
+            float u1 = 0.f, v1 = 0.f;
+            if (k + 1 < n) {
+                u1 = (float)cu[k + 1];
+                v1 = (float)cv[k + 1];
+            }
+            uv32[k] = make_float4((float)u, (float)v, u1, v1);
+        }
     }
 }
 
@@ -145,12 +154,14 @@ extern "C" int nbcs_spline_pack_uv(const double* cu, const double* cv, int64_t n
 {
     if (n < 0 || (n > 0 && (!cu || !cv || !coef_uv)))
         return set_error(NBCS_ERR_INVALID, "pack_uv: bad arguments");
+    if ((reinterpret_cast<uintptr_t>(coef_uv) | reinterpret_cast<uintptr_t>(coef_uv32)) & 15)
+        return set_error(NBCS_ERR_INVALID, "pack_uv: outputs must be 16-byte aligned");
     if (n == 0) return NBCS_OK;
     long blocks = (n + 255) / 256;
     long cap = (long)sm_count() * 16;
     if (blocks > cap) blocks = cap;
     pack_uv_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(
-        cu, cv, n, reinterpret_cast<double2*>(coef_uv), reinterpret_cast<float2*>(coef_uv32));
+        cu, cv, n, reinterpret_cast<double2*>(coef_uv), reinterpret_cast<float4*>(coef_uv32));
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }

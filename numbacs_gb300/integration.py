@@ -22,7 +22,7 @@ STATUS_NAMES = {0: "ok", 1: "masked", -2: "max_steps", -3: "step_underflow", -4:
 
 def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, atol=1e-8,
                     mask=None, *, precision="fp64", max_steps=100000, return_status=False,
-                    return_stats=False, out=None):
+                    return_stats=False, out=None, lanes_per_particle=0, blocks_per_sm=0):
     """Flow map at t0+T of every particle on the grid x by y -> (nx, ny, 2).
 
     Same positional signature and defaults as the reference.  Keyword-only
@@ -30,13 +30,16 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
     double; "mixed" = FP32 stages with compensated FP32-pair positions),
     ``max_steps`` (attempted-step limit), ``return_status`` (also return the
     per-particle int32 status), ``return_stats`` (also return (nx, ny, 3)
-    accepted / rejected / RHS-evaluation counts) and ``out`` (a preallocated
-    (nx, ny, 2) float64 CUDA tensor).
+    accepted / rejected / RHS-evaluation counts), ``out`` (a preallocated
+    (nx, ny, 2) float64 CUDA tensor), and the launch-shape knobs
+    ``lanes_per_particle`` (mixed spline path: 1, 2 or 4 lanes share one
+    particle's RHS; 0 = automatic) and ``blocks_per_sm`` (0 = one block per
+    particle tile).
 
     ``method="lsoda"`` raises NotImplementedError: only DOP853 runs on the GPU.
     Particles whose integration failed (step limit, step underflow, NaN) keep
-    their last position and, unless their status is requested, raise a
-    warning with the counts.
+    their last position; numpy callers that did not ask for the status get
+    a warning with the counts.
     """
     if method.lower() != "dop853":
         raise NotImplementedError("method=%r: only 'dop853' is implemented on the GPU" % method)
@@ -61,13 +64,15 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
     opts = _lib.NbcsOpts()
     opts.precision = _PREC[precision]
     opts.max_steps = int(max_steps)
+    opts.lanes_per_particle = int(lanes_per_particle)
+    opts.blocks_per_sm = int(blocks_per_sm)
     opts.stats = stats.data_ptr() if stats is not None else None
     L = _lib.load()
     _lib.check(L.nbcs_flowmap_grid_2d(flow.struct, float(t0), float(T), D.ptr(xd), nx, D.ptr(yd),
                                       ny, prm.ctypes.data_as(_lib._vp), len(prm), float(rtol),
                                       float(atol), D.ptr(md), D.ptr(out), D.ptr(status), opts,
                                       D.stream_ptr()))
-    if not return_status:
+    if not return_status and not as_torch:  # torch callers stay asynchronous
         bad = status[(status != 0) & (status != 1)]
         if bad.numel():
             vals, counts = torch.unique(bad, return_counts=True)

@@ -33,6 +33,7 @@
 #endif
 
 #include "../numbacs_gb300/csrc/dop853_tableau.h"
+#include "../numbacs_gb300/csrc/detmath.h"
 
 #define PI_D 3.141592653589793
 
@@ -142,7 +143,7 @@ static void rhs_spline(const orc_flow* fl, double t, const double* y, double* dy
         double yy = y[1];
         double u = orc_eval_spline_3d(fl->grid, fl->cu, fl->extrap, tt, xx, yy);
         double v = orc_eval_spline_3d(fl->grid, fl->cv, fl->extrap, tt, xx, yy);
-        dy[0] = p[0] * u * 180.0 / (PI_D * fl->r * cos(yy * PI_D / 180.0));
+        dy[0] = p[0] * u * 180.0 / (PI_D * fl->r * nbcs_cos_deg(yy));
         dy[1] = p[0] * v * 180.0 / (PI_D * fl->r);
     } else {
         double u = orc_eval_spline_3d(fl->grid, fl->cu, fl->extrap, tt, y[0], y[1]);
@@ -151,6 +152,9 @@ static void rhs_spline(const orc_flow* fl, double t, const double* y, double* dy
         dy[1] = p[0] * v;
     }
 }
+
+double orc_cos_deg(double d) { return nbcs_cos_deg(d); }
+double orc_root8(double x) { return nbcs_root8(x); }
 
 void orc_rhs(const orc_flow* flow, double t, const double* y, double* dy, const double* p)
 {
@@ -273,7 +277,7 @@ static double hinit(const orc_flow* fl, const double* p, double x, const double*
     der2 = sqrt(der2) / h;
     der12 = dmax(fabs(der2), sqrt(dnf));
     if (der12 <= 1.0e-15) h1 = dmax(1.0e-6, fabs(h) * 1.0e-3);
-    else h1 = pow(0.01 / der12, 1.0 / 8.0);
+    else h1 = nbcs_root8(0.01 / der12); /* (0.01/der12)^(1/iord), iord = 8 */
     h = dmin(100.0 * fabs(h), dmin(h1, hmax));
     return dsign(h, posneg);
 }
@@ -372,8 +376,9 @@ int orc_dop853(const orc_flow* fl, const double* p, double x, double xend,
         err = fabs(h) * err * sqrt(1.0 / (deno * (double)N2));
         if (isnan(err)) { status = ORC_NONFINITE; break; }
         /* new step size, fac1 <= hnew/h <= fac2 */
-        fac11 = pow(err, expo1);
-        fac = fac11 / pow(facold, beta);
+        /* err^expo1 with expo1 = 1/8 (beta = 0, so facold^beta = 1) */
+        fac11 = nbcs_root8(err);
+        fac = fac11;
         fac = dmax(facc2, dmin(facc1, fac / safe));
         hnew = h / fac;
         if (err <= 1.0) {

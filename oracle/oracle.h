@@ -42,6 +42,10 @@ typedef struct {
     const double* cv;
 } orc_flow;
 
+/* the deterministic helpers of detmath.h (exposed for their accuracy test) */
+double orc_cos_deg(double d);
+double orc_root8(double x);
+
 /* velocity fields (one RHS evaluation, reference direction convention) */
 void orc_rhs(const orc_flow* flow, double t, const double* y, double* dy, const double* p);
 

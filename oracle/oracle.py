@@ -78,6 +78,9 @@ def lib():
         L.orc_percentile.argtypes = [vp, i64, d]
         L.orc_percentile.restype = d
         L.orc_ridge_field.argtypes = [vp, vp, vp, i, vp, i, d, d, vp, vp]
+        for fn in (L.orc_cos_deg, L.orc_root8):
+            fn.argtypes = [d]
+            fn.restype = d
         _lib = L
     return _lib
 
@@ -195,6 +198,19 @@ def ftle_from_eig(eigval_max, T):
 def percentile(f, q):
     f = np.ascontiguousarray(f, np.float64).ravel()
     return lib().orc_percentile(_dp(f), f.size, float(q))
+
+
+def cos_deg(d):
+    return lib().orc_cos_deg(float(d))
+
+
+def root8(x):
+    return lib().orc_root8(float(x))
+
+
+def ridge_field(f, eigvec_max, x, y, sdd_thresh=0.0, percentile_=0):
+    """(r_pts (nx*ny, 2), ridge mask (nx, ny) bool, threshold) -- _ftle_ridges."""
+    return _ridge_field(f, eigvec_max, x, y, sdd_thresh, percentile_)
 
 
 def _ridge_field(f, eigvec_max, x, y, sdd_thresh=0.0, percentile_=0):

@@ -126,7 +126,7 @@ def test_ridge_mask_bit_identical(nb, orc, shape, pct, sdd):
     f = orc.ftle_from_eig(oev[..., 1], 5.0)
     e = np.ascontiguousarray(ovec[..., :, 1])
     r_pts, rb, _, _ = nb.extraction._ftle_ridges(f, e, x, y, sdd, pct)
-    orp, orb, _ = orc._ridge_field(f, e, x, y, sdd, pct)
+    orp, orb, _ = orc.ridge_field(f, e, x, y, sdd, pct)
     assert np.array_equal(rb, orb)
     assert np.array_equal(r_pts, orp)
     pts = nb.ftle_ridge_pts(f, e, x, y, sdd, pct)

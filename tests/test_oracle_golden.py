@@ -107,6 +107,15 @@ def test_percentile_nan_inf_rules(orc):
     assert orc.percentile(np.array([1.0, -np.inf, 3.0]), 100) == 3.0
 
 
+def test_deterministic_math_accuracy(orc):
+    # shared + - * / sqrt implementations: within ~1 ulp of libm
+    for d in np.concatenate([np.linspace(-400, 400, 20001), [0.0, 45.0, 90.0, -90.0, 180.0]]):
+        c, r = orc.cos_deg(d), np.cos(np.radians(d))
+        assert abs(c - r) <= 4.5e-16 * max(1.0, abs(r)) + 1e-16, d
+    for x in np.concatenate([np.geomspace(1e-300, 1e300, 2001), [0.0, 1.0]]):
+        assert abs(orc.root8(x) - x ** 0.125) <= 3e-16 * x ** 0.125, x
+
+
 def test_extrapolation_is_constant(orc):
     # extrap_mode="constant": outside the grid box the value on its boundary
     t, xs, u, v, pts = _spline_case()
