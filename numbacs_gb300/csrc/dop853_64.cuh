@@ -5,8 +5,17 @@
 // (called at integration.py:169-171) runs: HINIT initial step, error norm
 // err5^2/(err5^2 + 0.01 err3^2) scaling, safe = 0.9, fac1 = 0.333, fac2 = 6,
 // beta = 0, uround = 2.3e-16, no step-size increase right after a rejection.
-// Stage sums keep the published operand order and skip the zero tableau
-// entries; compiled with -fmad=false so results match the CPU oracle.
+//
+// Arithmetic: every stage sum keeps the published operand order (ascending
+// stage index, zero tableau entries skipped, stage 2 as (h*a21)*k1) and the
+// file is compiled with -fmad=false, so results match the CPU oracle bit for
+// bit apart from the library transcendentals of the analytic flows.
+//
+// Code shape: the twelve stages run as one rolled loop (the right-hand side is
+// instantiated once per solver, not twelve times -- the unrolled form was
+// instruction-fetch bound); stage derivatives live in this thread's column of
+// shared memory and the tableau in constant memory.  The derivative at the new
+// point after an accepted step (FSAL) is the next step's stage 0.
 #pragma once
 
 #include "detmath.h"
@@ -14,6 +23,35 @@
 #include "nbcs_internal.cuh"
 
 namespace nbcs {
+
+constexpr int kThreads64 = 128;
+
+__constant__ double kA64[12][12] = {
+    {0.0},
+    {DP853_A_2_1},
+    {DP853_A_3_1, DP853_A_3_2},
+    {DP853_A_4_1, DP853_A_4_2, DP853_A_4_3},
+    {DP853_A_5_1, DP853_A_5_2, DP853_A_5_3, DP853_A_5_4},
+    {DP853_A_6_1, DP853_A_6_2, DP853_A_6_3, DP853_A_6_4, DP853_A_6_5},
+    {DP853_A_7_1, DP853_A_7_2, DP853_A_7_3, DP853_A_7_4, DP853_A_7_5, DP853_A_7_6},
+    {DP853_A_8_1, DP853_A_8_2, DP853_A_8_3, DP853_A_8_4, DP853_A_8_5, DP853_A_8_6, DP853_A_8_7},
+    {DP853_A_9_1, DP853_A_9_2, DP853_A_9_3, DP853_A_9_4, DP853_A_9_5, DP853_A_9_6, DP853_A_9_7,
+     DP853_A_9_8},
+    {DP853_A_10_1, DP853_A_10_2, DP853_A_10_3, DP853_A_10_4, DP853_A_10_5, DP853_A_10_6,
+     DP853_A_10_7, DP853_A_10_8, DP853_A_10_9},
+    {DP853_A_11_1, DP853_A_11_2, DP853_A_11_3, DP853_A_11_4, DP853_A_11_5, DP853_A_11_6,
+     DP853_A_11_7, DP853_A_11_8, DP853_A_11_9, DP853_A_11_10},
+    {DP853_A_12_1, DP853_A_12_2, DP853_A_12_3, DP853_A_12_4, DP853_A_12_5, DP853_A_12_6,
+     DP853_A_12_7, DP853_A_12_8, DP853_A_12_9, DP853_A_12_10, DP853_A_12_11},
+};
+__constant__ double kC64[12] = {0.0, DP853_C_2, DP853_C_3, DP853_C_4, DP853_C_5, DP853_C_6,
+                                DP853_C_7, DP853_C_8, DP853_C_9, DP853_C_10, DP853_C_11, 1.0};
+__constant__ double kB64[12] = {DP853_B_1, DP853_B_2, DP853_B_3, DP853_B_4, DP853_B_5, DP853_B_6,
+                                DP853_B_7, DP853_B_8, DP853_B_9, DP853_B_10, DP853_B_11,
+                                DP853_B_12};
+__constant__ double kE5_64[12] = {DP853_E5_1, DP853_E5_2, DP853_E5_3, DP853_E5_4,
+                                  DP853_E5_5, DP853_E5_6, DP853_E5_7, DP853_E5_8,
+                                  DP853_E5_9, DP853_E5_10, DP853_E5_11, DP853_E5_12};
 
 // Comparison-based min/max (a NaN operand propagates the same way as in the
 // CPU oracle; fmin/fmax would drop it).
@@ -24,63 +62,63 @@ struct Dop853Stats {
     int accepted, rejected, nfcn;
 };
 
-template <class Flow>
-__device__ __forceinline__ double dop853_hinit64(const Flow& fl, const Params& P, double x,
-                                                 const double* y, double posneg,
-                                                 const double* f0, double hmax, double rtol,
-                                                 double atol)
-{
-    double dnf = 0.0, dny = 0.0, sk, sqr, h, der2, der12, h1, y1[2], f1[2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        sk = atol + rtol * fabs(y[i]);
-        sqr = f0[i] / sk;
-        dnf += sqr * sqr;
-        sqr = y[i] / sk;
-        dny += sqr * sqr;
-    }
-    if (dnf <= 1.0e-10 || dny <= 1.0e-10) h = 1.0e-6;
-    else h = sqrt(dny / dnf) * 0.01;
-    h = dmin_(h, hmax);
-    h = posneg >= 0.0 ? fabs(h) : -fabs(h);
-#pragma unroll
-    for (int i = 0; i < 2; ++i) y1[i] = y[i] + h * f0[i];
-    fl(x + h, y1, f1, P);
-    der2 = 0.0;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        sk = atol + rtol * fabs(y[i]);
-        sqr = (f1[i] - f0[i]) / sk;
-        der2 += sqr * sqr;
-    }
-    der2 = sqrt(der2) / h;
-    der12 = dmax_(fabs(der2), sqrt(dnf));
-    if (der12 <= 1.0e-15) h1 = dmax_(1.0e-6, fabs(h) * 1.0e-3);
-    else h1 = nbcs_root8(0.01 / der12);
-    h = dmin_(100.0 * fabs(h), dmin_(h1, hmax));
-    return posneg >= 0.0 ? fabs(h) : -fabs(h);
-}
-
-// Integrate y over solver time [x, xend].  Returns an NBCS_PARTICLE_* code.
+// Integrate y over solver time [x, xend]; `kc` is this thread's shared-memory
+// column of stage derivatives (stride kThreads64).  Returns NBCS_PARTICLE_*.
 template <class Flow>
 __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double xend, double* y,
-                              double rtol, double atol, int nmax, Dop853Stats* st)
+                              double rtol, double atol, int nmax, double2* kc, Dop853Stats* st)
 {
     const double uround = 2.3e-16, safe = 0.9, facc1 = 1.0 / 0.333, facc2 = 1.0 / 6.0;
-    double k1[2], k2[2], k3[2], k4[2], k5[2], k6[2], k7[2], k8[2], k9[2], k10[2], yy1[2];
-    double facold = 1.0e-4;
-    double posneg = (xend - x) >= 0.0 ? 1.0 : -1.0;
-    double hmax, h, hnew, xph, err, err2, deno, fac, fac11, sk, erri, sqr;
+    const double posneg = (xend - x) >= 0.0 ? 1.0 : -1.0;
+    double yy[2], kk[2], h = 0.0, hnew, hmax, err, err2, deno, fac, fac11, sk, erri, sqr;
     bool last = false, reject = false;
     int nstep = 0, status = NBCS_PARTICLE_OK;
     st->accepted = st->rejected = st->nfcn = 0;
     if (xend == x) return NBCS_PARTICLE_OK;
-
-    fl(x, y, k1, P);
     hmax = fabs(xend - x);
-    h = dop853_hinit64(fl, P, x, y, posneg, k1, hmax, rtol, atol);
+
+    // HINIT (f0 = f(x, y) is also stage 0 of the first step); one RHS site
+    double f0[2] = {0.0, 0.0}, dnf = 0.0, dny = 0.0;
+#pragma unroll 1
+    for (int e = 0; e < 2; ++e) {
+#pragma unroll
+        for (int i = 0; i < 2; ++i) yy[i] = e ? y[i] + h * f0[i] : y[i];
+        fl(e ? x + h : x, yy, kk, P);
+        if (e == 0) {
+            f0[0] = kk[0];
+            f0[1] = kk[1];
+            kc[0] = make_double2(kk[0], kk[1]);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                sk = atol + rtol * fabs(y[i]);
+                sqr = f0[i] / sk;
+                dnf += sqr * sqr;
+                sqr = y[i] / sk;
+                dny += sqr * sqr;
+            }
+            if (dnf <= 1.0e-10 || dny <= 1.0e-10) h = 1.0e-6;
+            else h = sqrt(dny / dnf) * 0.01;
+            h = dmin_(h, hmax);
+            h = posneg >= 0.0 ? fabs(h) : -fabs(h);
+        } else {
+            double der2 = 0.0, der12, h1;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                sk = atol + rtol * fabs(y[i]);
+                sqr = (kk[i] - f0[i]) / sk;
+                der2 += sqr * sqr;
+            }
+            der2 = sqrt(der2) / h;
+            der12 = dmax_(fabs(der2), sqrt(dnf));
+            if (der12 <= 1.0e-15) h1 = dmax_(1.0e-6, fabs(h) * 1.0e-3);
+            else h1 = nbcs_root8(0.01 / der12);  // (0.01/der12)^(1/8)
+            h = dmin_(100.0 * fabs(h), dmin_(h1, hmax));
+            h = posneg >= 0.0 ? fabs(h) : -fabs(h);
+        }
+    }
     st->nfcn += 2;
 
+    bool fsal = false;  // stage 0 (the derivative at the new point) still to evaluate
     for (;;) {
         if (nstep > nmax) { status = NBCS_PARTICLE_MAX_STEPS; break; }
         if (0.1 * fabs(h) <= fabs(x) * uround) { status = NBCS_PARTICLE_STEP_UNDERFLOW; break; }
@@ -89,78 +127,61 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
             last = true;
         }
         nstep++;
+#pragma unroll 1
+        for (int s = fsal ? 0 : 1; s < 12; ++s) {
+            if (s == 0) {
+                yy[0] = y[0];
+                yy[1] = y[1];
+            } else if (s == 1) {
+                const double2 k1 = kc[0];
+                yy[0] = y[0] + h * DP853_A_2_1 * k1.x;
+                yy[1] = y[1] + h * DP853_A_2_1 * k1.y;
+            } else {
+                double a0 = 0.0, a1 = 0.0;
 #pragma unroll
-        for (int i = 0; i < 2; ++i) yy1[i] = y[i] + h * DP853_A_2_1 * k1[i];
-        fl(x + DP853_C_2 * h, yy1, k2, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i) yy1[i] = y[i] + h * (DP853_A_3_1 * k1[i] + DP853_A_3_2 * k2[i]);
-        fl(x + DP853_C_3 * h, yy1, k3, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i) yy1[i] = y[i] + h * (DP853_A_4_1 * k1[i] + DP853_A_4_3 * k3[i]);
-        fl(x + DP853_C_4 * h, yy1, k4, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_5_1 * k1[i] + DP853_A_5_3 * k3[i] + DP853_A_5_4 * k4[i]);
-        fl(x + DP853_C_5 * h, yy1, k5, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_6_1 * k1[i] + DP853_A_6_4 * k4[i] + DP853_A_6_5 * k5[i]);
-        fl(x + DP853_C_6 * h, yy1, k6, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_7_1 * k1[i] + DP853_A_7_4 * k4[i] + DP853_A_7_5 * k5[i]
-                                 + DP853_A_7_6 * k6[i]);
-        fl(x + DP853_C_7 * h, yy1, k7, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_8_1 * k1[i] + DP853_A_8_4 * k4[i] + DP853_A_8_5 * k5[i]
-                                 + DP853_A_8_6 * k6[i] + DP853_A_8_7 * k7[i]);
-        fl(x + DP853_C_8 * h, yy1, k8, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_9_1 * k1[i] + DP853_A_9_4 * k4[i] + DP853_A_9_5 * k5[i]
-                                 + DP853_A_9_6 * k6[i] + DP853_A_9_7 * k7[i] + DP853_A_9_8 * k8[i]);
-        fl(x + DP853_C_9 * h, yy1, k9, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_10_1 * k1[i] + DP853_A_10_4 * k4[i] + DP853_A_10_5 * k5[i]
-                                 + DP853_A_10_6 * k6[i] + DP853_A_10_7 * k7[i] + DP853_A_10_8 * k8[i]
-                                 + DP853_A_10_9 * k9[i]);
-        fl(x + DP853_C_10 * h, yy1, k10, P);
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_11_1 * k1[i] + DP853_A_11_4 * k4[i] + DP853_A_11_5 * k5[i]
-                                 + DP853_A_11_6 * k6[i] + DP853_A_11_7 * k7[i] + DP853_A_11_8 * k8[i]
-                                 + DP853_A_11_9 * k9[i] + DP853_A_11_10 * k10[i]);
-        fl(x + DP853_C_11 * h, yy1, k2, P);
-        xph = x + h;
-#pragma unroll
-        for (int i = 0; i < 2; ++i)
-            yy1[i] = y[i] + h * (DP853_A_12_1 * k1[i] + DP853_A_12_4 * k4[i] + DP853_A_12_5 * k5[i]
-                                 + DP853_A_12_6 * k6[i] + DP853_A_12_7 * k7[i] + DP853_A_12_8 * k8[i]
-                                 + DP853_A_12_9 * k9[i] + DP853_A_12_10 * k10[i]
-                                 + DP853_A_12_11 * k2[i]);
-        fl(xph, yy1, k3, P);
-        st->nfcn += 11;
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            k4[i] = DP853_B_1 * k1[i] + DP853_B_6 * k6[i] + DP853_B_7 * k7[i] + DP853_B_8 * k8[i]
-                    + DP853_B_9 * k9[i] + DP853_B_10 * k10[i] + DP853_B_11 * k2[i]
-                    + DP853_B_12 * k3[i];
-            k5[i] = y[i] + h * k4[i];
+                for (int j = 0; j < 11; ++j) {
+                    if (j < s) {
+                        const double c = kA64[s][j];
+                        if (c != 0.0) {
+                            const double2 kj = kc[j * kThreads64];
+                            a0 = a0 + c * kj.x;
+                            a1 = a1 + c * kj.y;
+                        }
+                    }
+                }
+                yy[0] = y[0] + h * a0;
+                yy[1] = y[1] + h * a1;
+            }
+            fl(x + kC64[s] * h, yy, kk, P);
+            kc[s * kThreads64] = make_double2(kk[0], kk[1]);
         }
+        fsal = false;
+        st->nfcn += 11;
+        double b[2] = {0.0, 0.0}, e5[2] = {0.0, 0.0}, ynew[2];
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            const double2 kj = kc[j * kThreads64];
+            if (kB64[j] != 0.0) {
+                b[0] = b[0] + kB64[j] * kj.x;
+                b[1] = b[1] + kB64[j] * kj.y;
+            }
+            if (kE5_64[j] != 0.0) {
+                e5[0] = e5[0] + kE5_64[j] * kj.x;
+                e5[1] = e5[1] + kE5_64[j] * kj.y;
+            }
+        }
+        const double2 k1 = kc[0], k9 = kc[8 * kThreads64], k12 = kc[11 * kThreads64];
+        const double k1v[2] = {k1.x, k1.y}, k9v[2] = {k9.x, k9.y}, k12v[2] = {k12.x, k12.y};
         err = 0.0;
         err2 = 0.0;
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
-            sk = atol + rtol * dmax_(fabs(y[i]), fabs(k5[i]));
-            erri = k4[i] - DP853_BHH1 * k1[i] - DP853_BHH2 * k9[i] - DP853_BHH3 * k3[i];
+            ynew[i] = y[i] + h * b[i];
+            sk = atol + rtol * dmax_(fabs(y[i]), fabs(ynew[i]));
+            erri = b[i] - DP853_BHH1 * k1v[i] - DP853_BHH2 * k9v[i] - DP853_BHH3 * k12v[i];
             sqr = erri / sk;
             err2 += sqr * sqr;
-            erri = DP853_E5_1 * k1[i] + DP853_E5_6 * k6[i] + DP853_E5_7 * k7[i] + DP853_E5_8 * k8[i]
-                   + DP853_E5_9 * k9[i] + DP853_E5_10 * k10[i] + DP853_E5_11 * k2[i]
-                   + DP853_E5_12 * k3[i];
-            sqr = erri / sk;
+            sqr = e5[i] / sk;
             err += sqr * sqr;
         }
         deno = err + 0.01 * err2;
@@ -168,20 +189,16 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
         err = fabs(h) * err * sqrt(1.0 / (deno * 2.0));
         if (isnan(err)) { status = NBCS_PARTICLE_NONFINITE; break; }
         fac11 = nbcs_root8(err);  // err^(1/8)
-        fac = fac11;  // beta = 0: the Lund stabilisation factor facold^beta is 1
+        fac = fac11;              // beta = 0: the Lund factor facold^beta is 1
         fac = dmax_(facc2, dmin_(facc1, fac / safe));
         hnew = h / fac;
         if (err <= 1.0) {
-            facold = dmax_(err, 1.0e-4);
             st->accepted++;
-            fl(xph, k5, k4, P);
-            st->nfcn++;
-#pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                k1[i] = k4[i];
-                y[i] = k5[i];
-            }
-            x = xph;
+            st->nfcn++;  // the derivative at the new point (next step's stage 0)
+            y[0] = ynew[0];
+            y[1] = ynew[1];
+            x = x + h;
+            fsal = true;
             if (last) break;
             if (fabs(hnew) > hmax) hnew = posneg * hmax;
             if (reject) hnew = posneg * dmin_(fabs(hnew), fabs(h));
@@ -194,7 +211,6 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
         }
         h = hnew;
     }
-    (void)facold;
     return status;
 }
 

@@ -162,8 +162,8 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
     for (;;) {
         if (nstep > nmax) { status = NBCS_PARTICLE_MAX_STEPS; break; }
         float rem = f2_minus(xend, x);
-        // time is a compensated pair: resolution ~2^-44 relative
-        if (0.1f * fabsf(h) <= fabsf(x.hi) * 1.0e-13f) { status = NBCS_PARTICLE_STEP_UNDERFLOW; break; }
+        // time is a compensated pair: a step below ~2^-48 |t| no longer advances it
+        if (fabsf(h) <= fabsf(x.hi) * 3.6e-15f) { status = NBCS_PARTICLE_STEP_UNDERFLOW; break; }
         if ((1.01f * h - rem) * posneg > 0.f) {
             h = rem;
             last = true;

@@ -10,12 +10,14 @@
 namespace nbcs {
 
 template <class Flow>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kThreads64)
 flowmap64_kernel(Flow fl, Params P, double ts, double te, const double* __restrict__ x,
                  const double* __restrict__ y, int nx, int ny, const uint8_t* __restrict__ mask,
                  double* __restrict__ out, int32_t* __restrict__ status,
                  int32_t* __restrict__ stats, double rtol, double atol, int nmax)
 {
+    __shared__ double2 ks[12 * kThreads64];
+    double2* kc = ks + threadIdx.x;
     const long n = (long)nx * ny;
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += (long)gridDim.x * blockDim.x) {
@@ -26,7 +28,7 @@ flowmap64_kernel(Flow fl, Params P, double ts, double te, const double* __restri
         if (!(mask && mask[k])) {
             yv[0] = x[i];
             yv[1] = y[j];
-            st = dop853_solve64(fl, P, ts, te, yv, rtol, atol, nmax, &s);
+            st = dop853_solve64(fl, P, ts, te, yv, rtol, atol, nmax, kc, &s);
         }
         reinterpret_cast<double2*>(out)[k] = make_double2(yv[0], yv[1]);
         if (status) status[k] = st;
@@ -57,9 +59,12 @@ struct Launch64 {
     int operator()(const Flow& fl) const
     {
         const long n = (long)a->nx * a->ny;
-        int threads = a->threads > 0 ? a->threads : 128;
-        if (threads > 128) threads = 128;
+        const int threads = kThreads64;  // the stage-derivative columns are sized for it
         long blocks = (n + threads - 1) / threads;
+        if (a->blocks_per_sm > 0) {
+            long cap = (long)sm_count() * a->blocks_per_sm;
+            if (blocks > cap) blocks = cap;
+        }
         if (blocks > (1L << 30)) blocks = 1L << 30;
         flowmap64_kernel<<<(unsigned)blocks, threads, 0, a->stream>>>(
             fl, a->P, a->ts, a->te, a->x, a->y, a->nx, a->ny, a->mask, a->out, a->status,

@@ -36,13 +36,22 @@ struct FlowDG32 {
         const float* p = P.v;
         float tt = p[0] * (th + ts);
         float x = yh[0] + ys[0], y = yh[1] + ys[1];
+        // x - 1, x - 2 and the reflected y from the pair (the hi-part
+        // differences are exact near the walls) keep the sine arguments at
+        // FP32 relative accuracy
+        float xm1 = (yh[0] - 1.0f) + ys[0], xm2 = (yh[0] - 2.0f) + ys[0];
         float a = p[2] * sinf(fmaf(p[4], tt, p[5]));
         float b = fmaf(-2.0f, a, 1.0f);
-        float w = fmaf(a * x, x - 2.0f, x - 1.0f);  // f - 1
+        float w = fmaf(a * x, xm2, xm1);  // f - 1
         float df = fmaf(2.0f * a, x, b);
         float sw, cw, sy, cy;
         sincospif(w, &sw, &cw);  // sin(pi f) = -sw, cos(pi f) = -cw
-        sincospif(y, &sy, &cy);
+        if (yh[1] > 0.5f) {      // sin(pi y) = sin(pi (1 - y)), cos(pi y) = -cos(pi (1 - y))
+            sincospif((1.0f - yh[1]) - ys[1], &sy, &cy);
+            cy = -cy;
+        } else {
+            sincospif(y, &sy, &cy);
+        }
         const float piA = 3.14159265358979f * p[1];
         dy[0] = p[0] * fmaf(piA * sw, cy, -p[3] * x);
         dy[1] = p[0] * fmaf(-piA * cw * sy, df, -p[3] * y);
@@ -106,15 +115,17 @@ inline SplineGridF make_grid_f(const double* g)
     return s;
 }
 
-// Cell index and offset t in [0, 1] of the coordinate vh + vs on one axis.
-// extrap_mode "constant": coordinates outside [a, b] are clamped to the ends.
+// Cell index and offset t of the coordinate vh + vs on one axis.  The cell is
+// picked from the rounded coordinate, the offset is formed from the pair
+// (so t may sit a rounding error outside [0, 1] next to a knot, where the two
+// cubic pieces agree), and extrap_mode "constant" clamps the *precise* offset
+// at the two ends of the grid so the clamped field stays continuous.
 __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, float* t)
 {
     float u = ((vh + vs) - A.a_h) * A.dinv;
     if (u != u) { *t = u; return 0; }  // NaN propagates
-    if (!(u > 0.0f)) { *t = 0.0f; return 0; }
-    if (u >= (float)(A.n - 1)) { *t = 1.0f; return A.n - 2; }
-    int i = min((int)u, A.n - 2);
+    const float top = (float)(A.n - 2);
+    int i = (int)floorf(fminf(fmaxf(u, 0.0f), top));
     float fi = (float)i;
     // node position a + i*d as s + lo (exact product, two-sum on the hi parts)
     float p = __fmul_rn(fi, A.d_h);
@@ -125,7 +136,10 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
     float err = __fadd_rn(__fsub_rn(A.a_h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
     float lo = err + (e + A.a_l);
     float r = __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
-    *t = r * A.dinv;
+    float tt = r * A.dinv;
+    if (i == 0) tt = fmaxf(tt, 0.0f);
+    if (i == A.n - 2) tt = fminf(tt, 1.0f);
+    *t = tt;
     return i;
 }
 

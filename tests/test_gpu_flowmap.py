@@ -148,21 +148,57 @@ def test_flowmap_deterministic(nb):
         assert np.array_equal(a, b), prec
 
 
-def test_mixed_precision_vs_converged_truth(nb, orc):
-    # the mixed path is judged against an FP64 solution converged to 1e-12
+def _err_stats(fm, truth):
+    e = np.abs(fm - truth).max(axis=-1).ravel()
+    return {"mean": e.mean(), "median": np.median(e), "q99": np.quantile(e, 0.99), "max": e.max()}
+
+
+@pytest.mark.parametrize("rtol", [1e-6, 1e-7])
+def test_mixed_precision_vs_converged_truth(nb, orc, rtol):
+    """Double gyre, mixed path against an FP64 solution converged to rtol
+    1e-12.  Its FP32 right-hand side carries ~1e-7 relative error, which the
+    gyre's stretching amplifies to a floor of ~1e-6 in the end points: the
+    median error must stay within 1e-6 of the domain extent (2), the 99th
+    percentile within 1e-5 of it, and at rtol 1e-6, where truncation error
+    dominates, within 3x of the plain FP64 path's."""
     x, y = np.linspace(0, 2, 81), np.linspace(0, 1, 41)
     fl, p, _ = nb.get_predefined_flow("double_gyre", int_direction=-1.0)
     truth = orc.flowmap_grid_2D(orc.double_gyre(), 0.0, -10.0, x, y, p, rtol=1e-12, atol=1e-14)
-    plain = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, rtol=1e-8, atol=1e-10)
-    mixed = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, rtol=1e-8, atol=1e-10, precision="mixed")
-    e_plain = np.abs(plain - truth).max()
-    e_mixed = np.abs(mixed - truth).max()
-    assert e_plain <= 2e-6
-    assert e_mixed <= 2e-6, e_mixed  # 1e-6 of the domain extent (2)
-    # at the default tolerance both controllers stay within the same bound of each other
-    m6 = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, precision="mixed")
-    p6 = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p)
-    assert np.median(np.abs(m6 - p6)) < 1e-7
+    plain, sp = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, rtol=rtol, atol=1e-2 * rtol,
+                                   return_status=True)
+    mixed, sm = nb.flowmap_grid_2D(fl, 0.0, -10.0, x, y, p, rtol=rtol, atol=1e-2 * rtol,
+                                   precision="mixed", return_status=True)
+    assert (sp == 0).all() and (sm == 0).all()
+    ep, em = _err_stats(plain, truth), _err_stats(mixed, truth)
+    assert em["median"] <= 2e-6, (em, ep)
+    assert em["q99"] <= 2e-5, (em, ep)
+    if rtol >= 1e-6:
+        assert em["q99"] <= 3 * ep["q99"], (em, ep)
+
+
+def test_mixed_precision_geo_vs_fp64(nb, orc):
+    # spline flow, spherical: mixed vs plain at the same rtol, both vs a tight FP64 solve
+    t, lon, lat, U, V = _small_geo(orc)
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, U, V)
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    xf = np.linspace(lon[0], lon[-1], 81)
+    yf = np.linspace(lat[0], lat[-1], 41)
+    p = np.array([-1.0])
+    truth = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, rtol=1e-12, atol=1e-14)
+    for rtol in (1e-6, 1e-7):
+        plain = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, rtol=rtol, atol=1e-2 * rtol)
+        mixed, st = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, rtol=rtol, atol=1e-2 * rtol,
+                                       precision="mixed", return_status=True)
+        assert (st == 0).all()
+        ep, em = _err_stats(plain, truth), _err_stats(mixed, truth)
+        assert em["median"] <= 3 * ep["median"] + 1e-9, (rtol, em, ep)
+        assert em["q99"] <= 3 * ep["q99"] + 1e-8, (rtol, em, ep)
+    # a particle at (1e-12, 4e-15): sk ~ atol, so HINIT proposes h ~ 1e-12; the
+    # compensated time pair must still advance (no spurious step underflow)
+    one = np.array([1.4210854715202004e-12]), np.array([4.440892098500626e-15])
+    m1, s1 = nb.flowmap_grid_2D(fl, 180.0, -72.0, *one, p, precision="mixed", return_status=True)
+    d1, _ = nb.flowmap_grid_2D(fl, 180.0, -72.0, *one, p, return_status=True)
+    assert s1.item() == 0 and np.abs(m1 - d1).max() < 1e-3
 
 
 def test_status_codes(nb):
