@@ -158,6 +158,25 @@ int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int
                    uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
                    void* scratch, size_t scratch_bytes, void* stream);
 
+/* Allocation-free variant of nbcs_ridge_pts.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory -- a
+ * plugin whose host program keeps all cudaMalloc calls to itself, or a caller
+ * binding this library through a thin FFI with no device allocator of its
+ * own.  Same arguments and results as nbcs_ridge_pts, minus the scratch: the
+ * scratch is a fixed array compiled into the library (about 8.5 MB, see
+ * nbcs_ridge_noalloc_scratch_bytes), which every GPU that loads the library
+ * holds until the process exits.  Grids above NBCS_RIDGE_NOALLOC_MAX_POINTS
+ * points are rejected with NBCS_ERR_INVALID.  The first call on a device looks
+ * up the array's device address with that device current; make it before any
+ * stream capture.  All calls share the array, so calls whose work overlaps on
+ * the GPU race on it. */
+#define NBCS_RIDGE_NOALLOC_MAX_POINTS (1L << 23)
+size_t nbcs_ridge_noalloc_scratch_bytes(void);
+int nbcs_ridge_pts_noalloc(const double* f, const double* evec_max, const double* x, int32_t nx,
+                           const double* y, int32_t ny, double sdd_thresh, double percentile,
+                           uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
+                           void* stream);
+
 /* ------------------------------------------------------------ measurement */
 /* No counterpart in the reference (which has no GPU path). */
 

@@ -55,6 +55,9 @@ SIGNATURES = {
     "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
                                       _vp, _sz, _vp]),
+    "nbcs_ridge_noalloc_scratch_bytes": (_sz, []),
+    "nbcs_ridge_pts_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp,
+                                              _vp, _vp, _vp]),
     "nbcs_launch_count": (ctypes.c_ulonglong, []),
     "nbcs_probe_fma": (ctypes.c_int, [_i32, _i64, _vp, ctypes.POINTER(ctypes.c_double), _vp]),
 }

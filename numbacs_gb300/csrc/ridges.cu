@@ -20,6 +20,8 @@
 // Compiled with -fmad=false: the stencil arithmetic is the reference's.
 #include <math.h>
 
+#include <mutex>
+
 #include "nbcs_internal.cuh"
 
 namespace nbcs {
@@ -484,4 +486,72 @@ extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const dou
         R, mask, off, reinterpret_cast<double2*>(pts_out));
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free ridge extraction.
+//
+// Some callers cannot allocate device memory: a plugin whose host program
+// keeps every cudaMalloc to itself (for example inside its time-step loop), or
+// a caller that binds this library through a thin FFI and has no device
+// allocator of its own.  nbcs_ridge_pts_noalloc gives them ridge extraction
+// without a scratch argument: its scratch is the file-scope array below,
+// sized for grids of up to NBCS_RIDGE_NOALLOC_MAX_POINTS points (about 8.5 MB,
+// held by every GPU that loads the library until the process exits).
+//
+// The array's name is only a host-side stand-in, so the device address is
+// looked up with cudaGetSymbolAddress, once per device, on the first call made
+// with that device current (make that first call before any stream capture).
+// Every call shares the array and leaves its contents behind; the kernels
+// re-initialise everything they read (the selection state and histogram, the
+// per-block counts, offsets and mask), and calls whose work overlaps on the
+// GPU race on it.
+
+namespace nbcs {
+
+constexpr size_t align256c(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr long kNoallocBlocks = (NBCS_RIDGE_NOALLOC_MAX_POINTS + kRidgeTile - 1) / kRidgeTile;
+constexpr size_t kNoallocScratchBytes =
+    align256c(sizeof(SelScratch)) + align256c(sizeof(unsigned int) * kNoallocBlocks) +
+    align256c(sizeof(unsigned long long) * kNoallocBlocks) +
+    align256c((size_t)NBCS_RIDGE_NOALLOC_MAX_POINTS);
+
+static __device__ __align__(256) unsigned char g_ridge_noalloc_scratch[kNoallocScratchBytes];
+
+static int noalloc_scratch(void** out)
+{
+    static std::mutex mu;
+    static void* addr[64] = {nullptr};
+    int dev = 0;
+    NBCS_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(NBCS_ERR_INVALID, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        NBCS_CUDA_TRY(cudaGetSymbolAddress(&p, g_ridge_noalloc_scratch));
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return NBCS_OK;
+}
+
+}  // namespace nbcs
+
+extern "C" size_t nbcs_ridge_noalloc_scratch_bytes(void) { return nbcs::kNoallocScratchBytes; }
+
+extern "C" int nbcs_ridge_pts_noalloc(const double* f, const double* evec_max, const double* x,
+                                      int32_t nx, const double* y, int32_t ny, double sdd_thresh,
+                                      double percentile, uint8_t* mask_out, double* rpts_full,
+                                      double* pts_out, int64_t* n_out, void* stream)
+{
+    if (nx < 0 || ny < 0 || (long)nx * ny > NBCS_RIDGE_NOALLOC_MAX_POINTS)
+        return set_error(NBCS_ERR_INVALID,
+                         "ridge_pts_noalloc: %d x %d grid exceeds the fixed scratch limit of %ld "
+                         "points; use nbcs_ridge_pts with caller scratch",
+                         nx, ny, (long)NBCS_RIDGE_NOALLOC_MAX_POINTS);
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    return nbcs_ridge_pts(f, evec_max, x, nx, y, ny, sdd_thresh, percentile, mask_out, rpts_full,
+                          pts_out, n_out, scratch, kNoallocScratchBytes, stream);
 }
