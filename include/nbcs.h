@@ -116,6 +116,50 @@ int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T,
                          const uint8_t* mask, double* flowmap, int32_t* status,
                          const nbcs_opts* opts, void* stream);
 
+/* -------------------------------------------------------- batched fields */
+
+/* One FTLE field of a batched launch: what one flowmap_grid_2D call (plus an
+ * optional ftle_evec_2d) takes.  Replaces the reference's Python loop over t0
+ * values (examples/time_series/*.py) that calls flowmap_grid_2D and
+ * ftle_grid_2D once per field.  All pointers are device pointers. */
+typedef struct nbcs_field {
+    int32_t flow;      /* index into the batch's flows array */
+    int32_t nx, ny;
+    int32_t np;        /* number of params */
+    double params[NBCS_MAX_PARAMS];
+    double t0, T, rtol, atol;
+    double dx, dy;     /* grid spacing for the FTLE stencil */
+    const double* x;
+    const double* y;
+    const uint8_t* mask; /* nullable */
+    double* flowmap;     /* (nx, ny, 2) */
+    int32_t* status;     /* nullable */
+    double* ftle;        /* (nx, ny); NULL: no FTLE for this field */
+    double* evec_max;    /* (nx, ny, 2); used when ftle != NULL */
+} nbcs_field;
+
+/* Host-side handle of a prepared batch (filled by nbcs_batch_prepare). */
+typedef struct nbcs_batch {
+    void* scratch;       /* device memory holding the batch description */
+    int32_t nflows, nfields, precision, reserved;
+    int64_t total_chunks; /* 32-particle work units over all fields */
+    int64_t ftle_blocks;  /* 256-point FTLE work units */
+} nbcs_batch;
+
+size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields);
+/* Copy the flows and fields (host arrays) into `scratch` and fill `plan`.
+ * Reads host memory: not capturable; call once per batch layout. */
+int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const nbcs_field* fields,
+                       int32_t nfields, int32_t precision, void* scratch, size_t scratch_bytes,
+                       nbcs_batch* plan, void* stream);
+/* Integrate every particle of every field in one persistent launch (warps
+ * take 32-particle chunks from a shared counter, so fields of different sizes
+ * and lengths balance across the GPU), then run the FTLE/eigvec stencil of all
+ * fields in one launch.  Kernel launches only: capturable in a CUDA graph.
+ * opts: precision is taken from the plan; blocks_per_sm sets the persistent
+ * grid (0 = full occupancy); stats/step_model unused. */
+int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, void* stream);
+
 /* ------------------------------------------------------------ diagnostics */
 
 /* ftle_grid_2D (diagnostics.py:21-65): flowmap (nx,ny,2) -> ftle (nx,ny). */

@@ -34,6 +34,25 @@ class NbcsOpts(ctypes.Structure):
                 ("stats", ctypes.c_void_p), ("step_model", ctypes.c_void_p)]
 
 
+class NbcsField(ctypes.Structure):
+    """Mirror of ``struct nbcs_field``."""
+    _fields_ = [("flow", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+                ("np", ctypes.c_int32), ("params", ctypes.c_double * MAX_PARAMS),
+                ("t0", ctypes.c_double), ("T", ctypes.c_double), ("rtol", ctypes.c_double),
+                ("atol", ctypes.c_double), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("mask", ctypes.c_void_p),
+                ("flowmap", ctypes.c_void_p), ("status", ctypes.c_void_p),
+                ("ftle", ctypes.c_void_p), ("evec_max", ctypes.c_void_p)]
+
+
+class NbcsBatch(ctypes.Structure):
+    """Mirror of ``struct nbcs_batch``."""
+    _fields_ = [("scratch", ctypes.c_void_p), ("nflows", ctypes.c_int32),
+                ("nfields", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("total_chunks", ctypes.c_int64),
+                ("ftle_blocks", ctypes.c_int64)]
+
+
 # name -> (restype, argtypes)
 _vp, _d, _i32, _i64, _sz = ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t
 _FP = ctypes.POINTER(NbcsFlow)
@@ -55,6 +74,10 @@ SIGNATURES = {
     "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
                                       _vp, _sz, _vp]),
+    "nbcs_batch_scratch_bytes": (_sz, [_i32, _i32]),
+    "nbcs_batch_prepare": (ctypes.c_int, [_FP, _i32, ctypes.POINTER(NbcsField), _i32, _i32, _vp,
+                                          _sz, ctypes.POINTER(NbcsBatch), _vp]),
+    "nbcs_batch_run": (ctypes.c_int, [ctypes.POINTER(NbcsBatch), ctypes.POINTER(NbcsOpts), _vp]),
     "nbcs_ridge_noalloc_scratch_bytes": (_sz, []),
     "nbcs_ridge_pts_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp,
                                               _vp, _vp, _vp]),

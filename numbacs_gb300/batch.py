@@ -1,0 +1,151 @@
+"""Many FTLE fields in one persistent launch.
+
+The reference builds FTLE time series with a Python loop over t0 that calls
+``flowmap_grid_2D`` and ``ftle_grid_2D`` per field
+(examples/time_series/plot_dg_time_series.py,
+examples/time_series/plot_dg_numbacs_vs_scipy.py).  :class:`FTLEBatch` takes
+the whole list of fields -- any mix of flows, start times, integration
+lengths and grid sizes -- and integrates every particle of every field in one
+persistent kernel whose warps take 32-particle chunks from a shared counter
+(csrc/batch32.cu, csrc/batch64.cu), then computes all FTLE fields and their
+eigenvectors in one stencil launch.  The run is kernel launches only, so it is
+captured once in a CUDA graph and replayed.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _device as D
+from . import _lib
+from .flows import _check_callable_flow
+
+_PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+
+
+class Field:
+    """One FTLE field: the arguments of one flowmap_grid_2D call plus FTLE."""
+
+    def __init__(self, flow, t0, T, x, y, params, rtol=1e-6, atol=1e-8, mask=None, ftle=True):
+        self.flow = _check_callable_flow(flow)
+        self.t0, self.T = float(t0), float(T)
+        self.x, self.y = D.to_dev(x), D.to_dev(y)
+        self.params = np.ascontiguousarray(
+            params.cpu().numpy() if isinstance(params, torch.Tensor) else params, dtype=np.float64)
+        if not 1 <= len(self.params) <= _lib.MAX_PARAMS:
+            raise ValueError("params: 1..%d values" % _lib.MAX_PARAMS)
+        self.rtol, self.atol = float(rtol), float(atol)
+        self.mask = D.mask_to_dev(mask)
+        self.want_ftle = bool(ftle)
+        nx, ny = self.x.numel(), self.y.numel()
+        self.flowmap = D.empty((nx, ny, 2))
+        self.status = D.empty((nx, ny), torch.int32)
+        self.ftle = D.empty((nx, ny)) if ftle else None
+        self.evec = D.empty((nx, ny, 2)) if ftle else None
+        xs = self.x.cpu()
+        ys = self.y.cpu()
+        self.dx = float(xs[1] - xs[0]) if nx > 1 else 1.0
+        self.dy = float(ys[1] - ys[0]) if ny > 1 else 1.0
+
+    @property
+    def particles(self):
+        return self.x.numel() * self.y.numel()
+
+
+class FTLEBatch:
+    """A prepared batch of fields; ``run()`` recomputes every field in place.
+
+    ``precision`` is "mixed" or "fp64"; ``blocks_per_sm`` sets the persistent
+    grid (None: taken from the autotuner cache, tuning on first use; 0: full
+    occupancy); ``graph=True`` captures the run in a CUDA graph on first call.
+    """
+
+    def __init__(self, fields, precision="mixed", blocks_per_sm=None, graph=True, max_steps=100000):
+        D.require_cuda()
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.fields = list(fields)
+        if not self.fields:
+            raise ValueError("empty batch")
+        self.precision = precision
+        flows, index = [], {}
+        for f in self.fields:
+            if id(f.flow) not in index:
+                index[id(f.flow)] = len(flows)
+                flows.append(f.flow)
+        self._flows = flows
+        FlowArr = _lib.NbcsFlow * len(flows)
+        self._flow_arr = FlowArr(*[fl.struct for fl in flows])
+        FieldArr = _lib.NbcsField * len(self.fields)
+        arr = FieldArr()
+        for k, f in enumerate(self.fields):
+            s = arr[k]
+            s.flow = index[id(f.flow)]
+            s.nx, s.ny = f.x.numel(), f.y.numel()
+            s.np = len(f.params)
+            for q, v in enumerate(f.params):
+                s.params[q] = float(v)
+            s.t0, s.T, s.rtol, s.atol, s.dx, s.dy = f.t0, f.T, f.rtol, f.atol, f.dx, f.dy
+            s.x, s.y = f.x.data_ptr(), f.y.data_ptr()
+            s.mask = f.mask.data_ptr() if f.mask is not None else None
+            s.flowmap, s.status = f.flowmap.data_ptr(), f.status.data_ptr()
+            s.ftle = f.ftle.data_ptr() if f.ftle is not None else None
+            s.evec_max = f.evec.data_ptr() if f.evec is not None else None
+        self._field_arr = arr
+        L = _lib.load()
+        nbytes = L.nbcs_batch_scratch_bytes(len(flows), len(self.fields))
+        self._scratch = torch.empty(nbytes, dtype=torch.uint8, device=D.device())
+        self.plan = _lib.NbcsBatch()
+        _lib.check(L.nbcs_batch_prepare(self._flow_arr, len(flows), self._field_arr,
+                                        len(self.fields), _PREC[precision], D.ptr(self._scratch),
+                                        nbytes, ctypes.byref(self.plan), D.stream_ptr()))
+        self.max_steps = int(max_steps)
+        if blocks_per_sm is None:
+            from .autotune import tune_batch
+            blocks_per_sm = tune_batch(self)
+        self.blocks_per_sm = int(blocks_per_sm)
+        self.use_graph = graph
+        self._graph = None
+
+    @property
+    def particles(self):
+        return sum(f.particles for f in self.fields)
+
+    def _opts(self, blocks_per_sm=None):
+        o = _lib.NbcsOpts()
+        o.precision = _PREC[self.precision]
+        o.max_steps = self.max_steps
+        o.blocks_per_sm = self.blocks_per_sm if blocks_per_sm is None else int(blocks_per_sm)
+        return o
+
+    def launch(self, blocks_per_sm=None):
+        """Enqueue one run on the current stream (no graph)."""
+        _lib.check(_lib.load().nbcs_batch_run(ctypes.byref(self.plan), self._opts(blocks_per_sm),
+                                              D.stream_ptr()))
+
+    def capture(self):
+        """Capture one run into a CUDA graph (after one eager warm-up run)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.launch()
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch()
+        self._graph = g
+        return g
+
+    def run(self):
+        """Recompute every field (graph replay when enabled)."""
+        if self.use_graph:
+            if self._graph is None:
+                self.capture()
+            self._graph.replay()
+        else:
+            self.launch()
+        return self
+
+    def results(self):
+        """[(flowmap, ftle, evec_max, status)] device tensors, one per field."""
+        return [(f.flowmap, f.ftle, f.evec, f.status) for f in self.fields]

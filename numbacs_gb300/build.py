@@ -34,6 +34,8 @@ SOURCES = [
     ("spline.cu", ["-fmad=false"]),
     ("ridges.cu", ["-fmad=false"]),
     ("probe.cu", []),
+    ("batch32.cu", []),
+    ("batch64.cu", ["-fmad=false"]),
 ]
 
 

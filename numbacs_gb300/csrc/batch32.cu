@@ -1,0 +1,227 @@
+// Batched flow maps: many FTLE fields (different flows, t0, T, grid sizes) in
+// one persistent launch, and the host side of nbcs_batch_prepare / _run.
+//
+// The reference computes a time series of FTLE fields with a Python loop that
+// calls flowmap_grid_2D and ftle_grid_2D once per t0
+// (examples/time_series/plot_dg_time_series.py, plot_dg_numbacs_vs_scipy.py).
+// Here every particle of every field is one work item: warps of a persistent
+// grid take 32-particle chunks from a shared atomic counter, so a field with
+// long trajectories or a big grid spreads over the whole GPU instead of
+// leaving SMs idle at the end of a per-field launch.  The counter is reset by
+// a one-thread kernel at the start of every run, so a run is two or three
+// kernel launches and can be captured in a CUDA graph.
+#include <vector>
+
+#include "batch_common.cuh"
+#include "dop853_32.cuh"
+
+namespace nbcs {
+
+__global__ void batch_reset_kernel(BatchHeader* hdr) { hdr->counter = 0ull; }
+
+__global__ void __launch_bounds__(kBatchThreads)
+batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
+               const DevField* __restrict__ fields, int nfields, int nmax)
+{
+    __shared__ float2 ks[12 * kThreads32];
+    float2* kc = ks + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const long long total = hdr->total_chunks;
+    for (;;) {
+        unsigned long long c = 0ull;
+        if (lane == 0) c = atomicAdd(&hdr->counter, 1ull);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if ((long long)c >= total) break;
+        const int f = batch_find<true>(fields, nfields, (long long)c);
+        const DevField& F = fields[f];
+        const long n = (long)F.nx * F.ny;
+        const long p = (long)((long long)c - F.chunk0) * kBatchChunk + lane;
+        if (p >= n) continue;
+        const int i = (int)(p / F.ny), j = (int)(p - (long)i * F.ny);
+        double r0 = 0.0, r1 = 0.0;
+        int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
+        if (!(F.mask && F.mask[p])) {
+            ParamsF P;
+#pragma unroll
+            for (int q = 0; q < NBCS_MAX_PARAMS; ++q) P.v[q] = (float)F.P.v[q];
+            const F2 xs = f2_from_double(F.ts), xe = f2_from_double(F.te);
+            const float rtol = (float)F.rtol, atol = (float)F.atol;
+            F2 yv[2] = {f2_from_double(F.x[i]), f2_from_double(F.y[j])};
+            const DevFlow32& fl = flows[F.flow];
+            switch (fl.kind) {
+            case NBCS_FLOW_DOUBLE_GYRE:
+                st = dop853_solve32(FlowDG32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
+                break;
+            case NBCS_FLOW_BICKLEY:
+                st = dop853_solve32(FlowBickley32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj,
+                                    &nf);
+                break;
+            default:
+                if (fl.spherical == 1)
+                    st = dop853_solve32(FlowSpline32<1, 1>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv,
+                                        rtol, atol, nmax, kc, &a, &rj, &nf);
+                else if (fl.spherical == 2)
+                    st = dop853_solve32(FlowSpline32<2, 1>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv,
+                                        rtol, atol, nmax, kc, &a, &rj, &nf);
+                else
+                    st = dop853_solve32(FlowSpline32<0, 1>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv,
+                                        rtol, atol, nmax, kc, &a, &rj, &nf);
+                break;
+            }
+            r0 = f2_to_double(yv[0]);
+            r1 = f2_to_double(yv[1]);
+        }
+        reinterpret_cast<double2*>(F.out)[p] = make_double2(r0, r1);
+        if (F.status) F.status[p] = st;
+    }
+}
+
+static int persistent_blocks(const void* kernel, int threads, int blocks_per_sm)
+{
+    int per_sm = blocks_per_sm;
+    if (per_sm <= 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 4;
+    }
+    return per_sm * sm_count();
+}
+
+int launch_batch32(const BatchHeader* dev_hdr, const DevFlow32* flows, const DevField* fields,
+                   int nfields, int blocks_per_sm, int nmax, cudaStream_t s)
+{
+    BatchHeader* hdr = const_cast<BatchHeader*>(dev_hdr);
+    batch_reset_kernel<<<1, 1, 0, s>>>(hdr);
+    NBCS_LAUNCH_CHECK();
+    int blocks = persistent_blocks((const void*)batch32_kernel, kBatchThreads, blocks_per_sm);
+    batch32_kernel<<<blocks, kBatchThreads, 0, s>>>(hdr, flows, fields, nfields, nmax);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+int batch_blocks_for(const void* kernel, int blocks_per_sm)
+{
+    return persistent_blocks(kernel, kBatchThreads, blocks_per_sm);
+}
+
+}  // namespace nbcs
+
+using namespace nbcs;
+
+extern "C" size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields)
+{
+    if (nflows < 1 || nfields < 1) return 0;
+    return batch_layout(nflows, nfields).total;
+}
+
+extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const nbcs_field* fields,
+                                  int32_t nfields, int32_t precision, void* scratch,
+                                  size_t scratch_bytes, nbcs_batch* plan, void* stream)
+{
+    if (!flows || !fields || !plan || nflows < 1 || nfields < 1)
+        return set_error(NBCS_ERR_INVALID, "batch_prepare: need >= 1 flow and >= 1 field");
+    if (precision != NBCS_PREC_FP64 && precision != NBCS_PREC_MIXED)
+        return set_error(NBCS_ERR_INVALID, "batch_prepare: unknown precision %d", precision);
+    const BatchLayout lay = batch_layout(nflows, nfields);
+    if (!scratch || scratch_bytes < lay.total || (reinterpret_cast<uintptr_t>(scratch) & 255))
+        return set_error(NBCS_ERR_SCRATCH, "batch_prepare: scratch needs %zu bytes, 256-aligned",
+                         lay.total);
+    std::vector<unsigned char> host(lay.total, 0);
+    BatchHeader* hdr = reinterpret_cast<BatchHeader*>(host.data());
+    DevFlow32* f32 = reinterpret_cast<DevFlow32*>(host.data() + lay.off_f32);
+    DevFlow64* f64 = reinterpret_cast<DevFlow64*>(host.data() + lay.off_f64);
+    DevField* df = reinterpret_cast<DevField*>(host.data() + lay.off_fields);
+    for (int k = 0; k < nflows; ++k) {
+        const nbcs_flow& fl = flows[k];
+        f32[k].kind = f64[k].kind = fl.kind;
+        f32[k].spherical = f64[k].spherical = fl.spherical;
+        if (fl.kind == NBCS_FLOW_SPLINE2D) {
+            f32[k].g = make_grid_f(fl.grid);
+            f64[k].g = make_grid(fl.grid);
+        }
+        f32[k].c = reinterpret_cast<const float4*>(fl.coef_uv32);
+        f64[k].c = reinterpret_cast<const double2*>(fl.coef_uv);
+        f32[k].deg_per_km = (float)(180.0 / (3.141592653589793 * fl.r));
+        f64[k].r = fl.r;
+    }
+    long long chunks = 0, blocks = 0;
+    for (int k = 0; k < nfields; ++k) {
+        const nbcs_field& F = fields[k];
+        if (F.flow < 0 || F.flow >= nflows)
+            return set_error(NBCS_ERR_INVALID, "batch field %d: flow index %d out of range", k, F.flow);
+        int rc = validate_flow(&flows[F.flow], F.params, F.np, precision);
+        if (rc) return rc;
+        if (F.nx < 0 || F.ny < 0 || ((long)F.nx * F.ny > 0 && (!F.x || !F.y || !F.flowmap)))
+            return set_error(NBCS_ERR_INVALID, "batch field %d: bad grid or NULL array", k);
+        if (!(F.rtol > 0.0) || !(F.atol > 0.0))
+            return set_error(NBCS_ERR_INVALID, "batch field %d: rtol/atol must be > 0", k);
+        if ((reinterpret_cast<uintptr_t>(F.flowmap) | reinterpret_cast<uintptr_t>(F.evec_max)) & 15)
+            return set_error(NBCS_ERR_INVALID, "batch field %d: outputs must be 16-byte aligned", k);
+        if (F.ftle && !F.evec_max)
+            return set_error(NBCS_ERR_INVALID, "batch field %d: ftle needs evec_max", k);
+        DevField& D = df[k];
+        D.flow = F.flow;
+        D.nx = F.nx;
+        D.ny = F.ny;
+        D.has_ftle = F.ftle != nullptr;
+        for (int q = 0; q < NBCS_MAX_PARAMS; ++q) D.P.v[q] = q < F.np ? F.params[q] : 0.0;
+        D.ts = F.params[0] * F.t0;  // t_eval = params[0] * linspace(t0, t0 + T, 2)
+        D.te = F.params[0] * (F.t0 + F.T);
+        D.rtol = F.rtol;
+        D.atol = F.atol;
+        D.den = 2.0 * fabs(F.T);
+        D.dx = F.dx;
+        D.dy = F.dy;
+        D.x = F.x;
+        D.y = F.y;
+        D.mask = F.mask;
+        D.out = F.flowmap;
+        D.status = F.status;
+        D.ftle = F.ftle;
+        D.evec = F.evec_max;
+        D.chunk0 = chunks;
+        D.block0 = blocks;
+        long n = (long)F.nx * F.ny;
+        chunks += (n + kBatchChunk - 1) / kBatchChunk;
+        if (F.ftle) blocks += (n + kFtleBlock - 1) / kFtleBlock;
+    }
+    hdr->counter = 0;
+    hdr->total_chunks = chunks;
+    hdr->nfields = nfields;
+    hdr->nflows = nflows;
+    NBCS_CUDA_TRY(cudaMemcpyAsync(scratch, host.data(), lay.total, cudaMemcpyHostToDevice,
+                                  as_stream(stream)));
+    // pageable source: the call returns once the bytes are staged, so `host` may go
+    plan->scratch = scratch;
+    plan->nflows = nflows;
+    plan->nfields = nfields;
+    plan->precision = precision;
+    plan->reserved = 0;
+    plan->total_chunks = chunks;
+    plan->ftle_blocks = blocks;
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, void* stream)
+{
+    if (!plan || !plan->scratch) return set_error(NBCS_ERR_INVALID, "batch_run: no plan");
+    const BatchLayout lay = batch_layout(plan->nflows, plan->nfields);
+    unsigned char* base = static_cast<unsigned char*>(plan->scratch);
+    const BatchHeader* hdr = reinterpret_cast<const BatchHeader*>(base);
+    const DevField* fields = reinterpret_cast<const DevField*>(base + lay.off_fields);
+    const int bps = opts ? opts->blocks_per_sm : 0;
+    const int nmax = (opts && opts->max_steps > 0) ? opts->max_steps : 100000;
+    cudaStream_t s = as_stream(stream);
+    int rc;
+    if (plan->total_chunks > 0) {
+        if (plan->precision == NBCS_PREC_MIXED)
+            rc = launch_batch32(hdr, reinterpret_cast<const DevFlow32*>(base + lay.off_f32), fields,
+                                plan->nfields, bps, nmax, s);
+        else
+            rc = launch_batch64(hdr, reinterpret_cast<const DevFlow64*>(base + lay.off_f64), fields,
+                                plan->nfields, bps, nmax, s);
+        if (rc) return rc;
+    }
+    if (plan->ftle_blocks > 0) return launch_ftle_batch(fields, plan->nfields, plan->ftle_blocks, s);
+    return NBCS_OK;
+}

@@ -1,0 +1,90 @@
+// Device-side description of a batched launch (nbcs_batch_prepare / _run).
+//
+// Scratch layout (each part 256-byte aligned):
+//   BatchHeader | DevFlow32[nflows] | DevFlow64[nflows] | DevField[nfields]
+// Fields are listed with the prefix of their 32-particle chunks (chunk0) and
+// of their 256-point FTLE blocks (block0), so a work unit finds its field by
+// binary search.
+#pragma once
+
+#include "flows32.cuh"
+#include "nbcs_internal.cuh"
+
+namespace nbcs {
+
+constexpr int kBatchChunk = 32;        // particles per work unit (one warp, one lane each)
+constexpr int kBatchThreads = 128;
+constexpr int kFtleBlock = 256;        // points per FTLE work unit
+
+struct BatchHeader {
+    unsigned long long counter;  // next chunk to hand out
+    long long total_chunks;
+    int nfields, nflows;
+};
+
+struct DevFlow32 {
+    int kind, spherical;
+    SplineGridF g;
+    const float4* c;
+    float deg_per_km;
+};
+
+struct DevFlow64 {
+    int kind, spherical;
+    SplineGrid g;
+    const double2* c;
+    double r;
+};
+
+struct DevField {
+    int flow, nx, ny, has_ftle;
+    double ts, te, rtol, atol;
+    double den, dx, dy;  // FTLE: 2|T| and grid spacing
+    Params P;
+    const double* x;
+    const double* y;
+    const uint8_t* mask;
+    double* out;
+    int32_t* status;
+    double* ftle;
+    double* evec;
+    long long chunk0, block0;
+};
+
+inline size_t batch_align(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct BatchLayout {
+    size_t off_f32, off_f64, off_fields, total;
+};
+
+inline BatchLayout batch_layout(int nflows, int nfields)
+{
+    BatchLayout L;
+    L.off_f32 = batch_align(sizeof(BatchHeader));
+    L.off_f64 = L.off_f32 + batch_align(sizeof(DevFlow32) * (size_t)nflows);
+    L.off_fields = L.off_f64 + batch_align(sizeof(DevFlow64) * (size_t)nflows);
+    L.total = L.off_fields + batch_align(sizeof(DevField) * (size_t)nfields);
+    return L;
+}
+
+// index of the last field whose prefix value is <= c
+template <bool CHUNKS>
+__device__ __forceinline__ int batch_find(const DevField* __restrict__ fields, int nf, long long c)
+{
+    int lo = 0, hi = nf - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        long long v = CHUNKS ? fields[mid].chunk0 : fields[mid].block0;
+        if (v <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+int launch_batch32(const BatchHeader* dev_hdr, const DevFlow32* flows, const DevField* fields,
+                   int nfields, int blocks_per_sm, int nmax, cudaStream_t s);
+int launch_batch64(const BatchHeader* dev_hdr, const DevFlow64* flows, const DevField* fields,
+                   int nfields, int blocks_per_sm, int nmax, cudaStream_t s);
+int launch_ftle_batch(const DevField* fields, int nfields, long long blocks, cudaStream_t s);
+
+}  // namespace nbcs

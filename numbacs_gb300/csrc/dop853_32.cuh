@@ -1,0 +1,242 @@
+// Mixed-precision DOP853 for one particle (shared by the single-field and
+// batched integrators).
+//
+// Same DOP853 method and dop853 step-size controller as the FP64 path
+// (dop853_64.cuh), but the stages and the RHS run on the FP32 pipe.  Particle
+// position and time are carried as compensated FP32 pairs (hi + lo, ~48-bit
+// significand) so that accumulating many steps keeps FP64-class accuracy; a
+// stage argument is handed to the RHS as the pair (hi, lo + h*sum) and the RHS
+// forms what it needs from it (flows32.cuh).
+//
+// Code shape (from the profile of the fully unrolled version, which was
+// instruction-fetch bound): the twelve stages run as one rolled loop so the
+// right-hand side is instantiated once; the stage derivatives live in shared
+// memory (one column per thread) and the tableau in constant memory.
+#pragma once
+
+#include "detmath.h"
+#include "dop853_tableau.h"
+#include "flows32.cuh"
+#include "nbcs_internal.cuh"
+
+namespace nbcs {
+
+#define F_(x) ((float)(x))
+// DP853 tableau, 0-based stage index: stage s uses kA32[s][j] for j < s.
+static __constant__ float kA32[12][12] = {
+    {0.f},
+    {F_(DP853_A_2_1)},
+    {F_(DP853_A_3_1), F_(DP853_A_3_2)},
+    {F_(DP853_A_4_1), F_(DP853_A_4_2), F_(DP853_A_4_3)},
+    {F_(DP853_A_5_1), F_(DP853_A_5_2), F_(DP853_A_5_3), F_(DP853_A_5_4)},
+    {F_(DP853_A_6_1), F_(DP853_A_6_2), F_(DP853_A_6_3), F_(DP853_A_6_4), F_(DP853_A_6_5)},
+    {F_(DP853_A_7_1), F_(DP853_A_7_2), F_(DP853_A_7_3), F_(DP853_A_7_4), F_(DP853_A_7_5),
+     F_(DP853_A_7_6)},
+    {F_(DP853_A_8_1), F_(DP853_A_8_2), F_(DP853_A_8_3), F_(DP853_A_8_4), F_(DP853_A_8_5),
+     F_(DP853_A_8_6), F_(DP853_A_8_7)},
+    {F_(DP853_A_9_1), F_(DP853_A_9_2), F_(DP853_A_9_3), F_(DP853_A_9_4), F_(DP853_A_9_5),
+     F_(DP853_A_9_6), F_(DP853_A_9_7), F_(DP853_A_9_8)},
+    {F_(DP853_A_10_1), F_(DP853_A_10_2), F_(DP853_A_10_3), F_(DP853_A_10_4), F_(DP853_A_10_5),
+     F_(DP853_A_10_6), F_(DP853_A_10_7), F_(DP853_A_10_8), F_(DP853_A_10_9)},
+    {F_(DP853_A_11_1), F_(DP853_A_11_2), F_(DP853_A_11_3), F_(DP853_A_11_4), F_(DP853_A_11_5),
+     F_(DP853_A_11_6), F_(DP853_A_11_7), F_(DP853_A_11_8), F_(DP853_A_11_9), F_(DP853_A_11_10)},
+    {F_(DP853_A_12_1), F_(DP853_A_12_2), F_(DP853_A_12_3), F_(DP853_A_12_4), F_(DP853_A_12_5),
+     F_(DP853_A_12_6), F_(DP853_A_12_7), F_(DP853_A_12_8), F_(DP853_A_12_9), F_(DP853_A_12_10),
+     F_(DP853_A_12_11)},
+};
+static __constant__ float kC32[12] = {0.f, F_(DP853_C_2), F_(DP853_C_3), F_(DP853_C_4), F_(DP853_C_5),
+                               F_(DP853_C_6), F_(DP853_C_7), F_(DP853_C_8), F_(DP853_C_9),
+                               F_(DP853_C_10), F_(DP853_C_11), 1.0f};
+static __constant__ float kB32[12] = {F_(DP853_B_1), F_(DP853_B_2), F_(DP853_B_3), F_(DP853_B_4),
+                               F_(DP853_B_5), F_(DP853_B_6), F_(DP853_B_7), F_(DP853_B_8),
+                               F_(DP853_B_9), F_(DP853_B_10), F_(DP853_B_11), F_(DP853_B_12)};
+static __constant__ float kE5_32[12] = {F_(DP853_E5_1), F_(DP853_E5_2), F_(DP853_E5_3), F_(DP853_E5_4),
+                                 F_(DP853_E5_5), F_(DP853_E5_6), F_(DP853_E5_7), F_(DP853_E5_8),
+                                 F_(DP853_E5_9), F_(DP853_E5_10), F_(DP853_E5_11), F_(DP853_E5_12)};
+// 3rd-order estimate weights b_j - bhh_j (bhh at stages 1, 9, 12)
+static __constant__ float kE3_32[12] = {F_(DP853_B_1 - DP853_BHH1), F_(DP853_B_2), F_(DP853_B_3),
+                                 F_(DP853_B_4), F_(DP853_B_5), F_(DP853_B_6), F_(DP853_B_7),
+                                 F_(DP853_B_8), F_(DP853_B_9 - DP853_BHH2), F_(DP853_B_10),
+                                 F_(DP853_B_11), F_(DP853_B_12 - DP853_BHH3)};
+#undef F_
+
+constexpr int kThreads32 = 128;
+
+// unevaluated sum hi + lo
+struct F2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ F2 f2_from_double(double d)
+{
+    float h = (float)d;
+    return {h, (float)(d - (double)h)};
+}
+
+__device__ __forceinline__ double f2_to_double(F2 a) { return (double)a.hi + (double)a.lo; }
+
+// a + (p + e): Knuth two-sum of the hi parts, low parts added to the error.
+__device__ __forceinline__ F2 f2_add(F2 a, float p, float e)
+{
+    float s = __fadd_rn(a.hi, p);
+    float bb = __fsub_rn(s, a.hi);
+    float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    err = __fadd_rn(err, __fadd_rn(a.lo, e));
+    float h = __fadd_rn(s, err);
+    return {h, __fsub_rn(err, __fsub_rn(h, s))};
+}
+
+// a + h*b with the product rounding error kept
+__device__ __forceinline__ F2 f2_axpy(F2 a, float h, float b)
+{
+    float p = __fmul_rn(h, b);
+    float e = fmaf(h, b, -p);
+    return f2_add(a, p, e);
+}
+
+__device__ __forceinline__ float f2_minus(F2 a, F2 b)  // (a - b) rounded to float
+{
+    return (a.hi - b.hi) + (a.lo - b.lo);
+}
+
+// Integrate one particle (y, as compensated pairs) over solver time [x, xend].
+// `kc` is this thread's shared-memory column of stage derivatives (stride
+// kThreads32).  Returns an NBCS_PARTICLE_* code.
+template <class Flow>
+__device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2* y, float rtol,
+                              float atol, int nmax, float2* kc, int* acc, int* rej, int* nfcn)
+{
+    const float safe = 0.9f, facc1 = (float)(1.0 / 0.333), facc2 = (float)(1.0 / 6.0);
+    const float span = f2_minus(xend, x);
+    const float posneg = span >= 0.f ? 1.f : -1.f;
+    const float hmax = fabsf(span);
+    float yh[2], ys[2], kk[2];
+    int nstep = 0, status = NBCS_PARTICLE_OK;
+    bool last = false, reject = false;
+    *acc = *rej = *nfcn = 0;
+    if (span == 0.f) return NBCS_PARTICLE_OK;
+
+    // HINIT: f0 = f(x, y), Euler probe f1 = f(x + h, y + h f0); one RHS site
+    float h = 0.f, dnf = 0.f, dny = 0.f, f0[2] = {0.f, 0.f};
+#pragma unroll 1
+    for (int e = 0; e < 2; ++e) {
+        yh[0] = y[0].hi;
+        yh[1] = y[1].hi;
+        ys[0] = e ? fmaf(h, f0[0], y[0].lo) : y[0].lo;
+        ys[1] = e ? fmaf(h, f0[1], y[1].lo) : y[1].lo;
+        fl(x.hi, e ? x.lo + h : x.lo, yh, ys, kk, P);
+        if (e == 0) {
+            f0[0] = kk[0];
+            f0[1] = kk[1];
+            kc[0] = make_float2(kk[0], kk[1]);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                float yv = y[i].hi + y[i].lo;
+                float sk = fmaf(rtol, fabsf(yv), atol);
+                float a = f0[i] / sk, b = yv / sk;
+                dnf = fmaf(a, a, dnf);
+                dny = fmaf(b, b, dny);
+            }
+            h = (dnf <= 1.0e-10f || dny <= 1.0e-10f) ? 1.0e-6f : sqrtf(dny / dnf) * 0.01f;
+            h = copysignf(fminf(h, hmax), posneg);
+        } else {
+            float der2 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                float sk = fmaf(rtol, fabsf(y[i].hi + y[i].lo), atol);
+                float a = (kk[i] - f0[i]) / sk;
+                der2 = fmaf(a, a, der2);
+            }
+            der2 = sqrtf(der2) / h;
+            float der12 = fmaxf(fabsf(der2), sqrtf(dnf));
+            float h1 = der12 <= 1.0e-15f ? fmaxf(1.0e-6f, fabsf(h) * 1.0e-3f)
+                                         : nbcs_root8f(0.01f / der12);
+            h = copysignf(fminf(100.0f * fabsf(h), fminf(h1, hmax)), posneg);
+        }
+    }
+    *nfcn += 2;
+
+    bool fsal = false;  // stage 0 (the derivative at the new point) still to evaluate
+    for (;;) {
+        if (nstep > nmax) { status = NBCS_PARTICLE_MAX_STEPS; break; }
+        float rem = f2_minus(xend, x);
+        // time is a compensated pair: a step below ~2^-48 |t| no longer advances it
+        if (fabsf(h) <= fabsf(x.hi) * 3.6e-15f) { status = NBCS_PARTICLE_STEP_UNDERFLOW; break; }
+        if ((1.01f * h - rem) * posneg > 0.f) {
+            h = rem;
+            last = true;
+        }
+        nstep++;
+        yh[0] = y[0].hi;
+        yh[1] = y[1].hi;
+#pragma unroll 1
+        for (int s = fsal ? 0 : 1; s < 12; ++s) {
+            float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+            for (int j = 0; j < 11; ++j) {
+                if (j < s) {
+                    const float c = kA32[s][j];
+                    const float2 kj = kc[j * kThreads32];
+                    a0 = fmaf(c, kj.x, a0);
+                    a1 = fmaf(c, kj.y, a1);
+                }
+            }
+            ys[0] = fmaf(h, a0, y[0].lo);
+            ys[1] = fmaf(h, a1, y[1].lo);
+            fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);
+            kc[s * kThreads32] = make_float2(kk[0], kk[1]);
+        }
+        fsal = false;
+        *nfcn += 11;
+        float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            const float2 kj = kc[j * kThreads32];
+            b[0] = fmaf(kB32[j], kj.x, b[0]);
+            b[1] = fmaf(kB32[j], kj.y, b[1]);
+            e5[0] = fmaf(kE5_32[j], kj.x, e5[0]);
+            e5[1] = fmaf(kE5_32[j], kj.y, e5[1]);
+            e3[0] = fmaf(kE3_32[j], kj.x, e3[0]);
+            e3[1] = fmaf(kE3_32[j], kj.y, e3[1]);
+        }
+        F2 ynew[2];
+        float err = 0.f, err2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            ynew[i] = f2_axpy(y[i], h, b[i]);
+            float yo = y[i].hi + y[i].lo, yn = ynew[i].hi + ynew[i].lo;
+            float sk = fmaf(rtol, fmaxf(fabsf(yo), fabsf(yn)), atol);
+            float q3 = e3[i] / sk, q5 = e5[i] / sk;
+            err2 = fmaf(q3, q3, err2);
+            err = fmaf(q5, q5, err);
+        }
+        float deno = fmaf(0.01f, err2, err);
+        if (deno <= 0.f) deno = 1.f;
+        err = fabsf(h) * err * rsqrtf(deno * 2.0f);
+        if (isnan(err)) { status = NBCS_PARTICLE_NONFINITE; break; }
+        float fac11 = nbcs_root8f(err);  // err^(1/8)
+        float fac = fmaxf(facc2, fminf(facc1, fac11 / safe));
+        float hnew = h / fac;
+        if (err <= 1.0f) {
+            ++*acc;
+            ++*nfcn;  // the derivative at the new point (next step's stage 0)
+            x = f2_add(x, h, 0.f);
+            y[0] = ynew[0];
+            y[1] = ynew[1];
+            fsal = true;
+            if (last) break;
+            if (fabsf(hnew) > hmax) hnew = posneg * hmax;
+            if (reject) hnew = posneg * fminf(fabsf(hnew), fabsf(h));
+            reject = false;
+        } else {
+            hnew = h / fminf(facc1, fac11 / safe);
+            reject = true;
+            if (*acc >= 1) ++*rej;
+            last = false;
+        }
+        h = hnew;
+    }
+    return status;
+}
+
+}  // namespace nbcs

@@ -26,7 +26,7 @@ namespace nbcs {
 
 constexpr int kThreads64 = 128;
 
-__constant__ double kA64[12][12] = {
+static __constant__ double kA64[12][12] = {
     {0.0},
     {DP853_A_2_1},
     {DP853_A_3_1, DP853_A_3_2},
@@ -44,12 +44,12 @@ __constant__ double kA64[12][12] = {
     {DP853_A_12_1, DP853_A_12_2, DP853_A_12_3, DP853_A_12_4, DP853_A_12_5, DP853_A_12_6,
      DP853_A_12_7, DP853_A_12_8, DP853_A_12_9, DP853_A_12_10, DP853_A_12_11},
 };
-__constant__ double kC64[12] = {0.0, DP853_C_2, DP853_C_3, DP853_C_4, DP853_C_5, DP853_C_6,
+static __constant__ double kC64[12] ={0.0, DP853_C_2, DP853_C_3, DP853_C_4, DP853_C_5, DP853_C_6,
                                 DP853_C_7, DP853_C_8, DP853_C_9, DP853_C_10, DP853_C_11, 1.0};
-__constant__ double kB64[12] = {DP853_B_1, DP853_B_2, DP853_B_3, DP853_B_4, DP853_B_5, DP853_B_6,
+static __constant__ double kB64[12] ={DP853_B_1, DP853_B_2, DP853_B_3, DP853_B_4, DP853_B_5, DP853_B_6,
                                 DP853_B_7, DP853_B_8, DP853_B_9, DP853_B_10, DP853_B_11,
                                 DP853_B_12};
-__constant__ double kE5_64[12] = {DP853_E5_1, DP853_E5_2, DP853_E5_3, DP853_E5_4,
+static __constant__ double kE5_64[12] ={DP853_E5_1, DP853_E5_2, DP853_E5_3, DP853_E5_4,
                                   DP853_E5_5, DP853_E5_6, DP853_E5_7, DP853_E5_8,
                                   DP853_E5_9, DP853_E5_10, DP853_E5_11, DP853_E5_12};
 

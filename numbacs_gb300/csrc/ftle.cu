@@ -10,6 +10,7 @@
 // the L1/L2 caches serve, so DRAM sees ~16 B read + 8 B (FTLE) or +16 B
 // (eigenvector) written per point.  Compiled with -fmad=false: the arithmetic
 // is the reference's, operation for operation.
+#include "batch_common.cuh"
 #include "nbcs_internal.cuh"
 
 namespace nbcs {
@@ -155,6 +156,45 @@ __global__ void ftle_from_eig_kernel(const double* __restrict__ ev, long n, long
         double e = ev[k * stride];
         ftle[k] = e > 1.0 ? log(e) / den : 0.0;
     }
+}
+
+// FTLE + eigvec_max of every field of a batch (fields without FTLE own no
+// blocks); one 256-thread block per 256-point unit of a field.
+__global__ void __launch_bounds__(kFtleBlock)
+ftle_batch_kernel(const DevField* __restrict__ fields, int nfields, long long total_blocks)
+{
+    for (long long b = blockIdx.x; b < total_blocks; b += gridDim.x) {
+        const int f = batch_find<false>(fields, nfields, b);
+        const DevField& F = fields[f];
+        const long n = (long)F.nx * F.ny;
+        const long k = (long)(b - F.block0) * kFtleBlock + threadIdx.x;
+        if (k >= n) continue;
+        int i, j;
+        double fv = 0.0;
+        double2 v = make_double2(0.0, 0.0);
+        if (interior(k, F.nx, F.ny, &i, &j) && !(F.mask && F.mask[k])) {
+            Grad g = grad_stencil(reinterpret_cast<const double2*>(F.out), k, F.ny, F.dx, F.dy);
+            double off = g.dxdx * g.dxdy + g.dydx * g.dydy;
+            double a = g.dxdx * g.dxdx + g.dydx * g.dydx;
+            double d = g.dxdy * g.dxdy + g.dydy * g.dydy;
+            double l0, l1, vx, vy;
+            sym2_eig(a, off, d, &l0, &l1, &vx, &vy);
+            if (l1 > 1.0) fv = log(l1) / F.den;
+            v = make_double2(vx, vy);
+        }
+        F.ftle[k] = fv;
+        reinterpret_cast<double2*>(F.evec)[k] = v;
+    }
+}
+
+int launch_ftle_batch(const DevField* fields, int nfields, long long blocks, cudaStream_t s)
+{
+    long long g = blocks;
+    long long cap = (long long)sm_count() * 32;
+    if (g > cap) g = cap;
+    ftle_batch_kernel<<<(unsigned)g, kFtleBlock, 0, s>>>(fields, nfields, blocks);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
 }
 
 static unsigned grid_for(long n, int threads)

@@ -79,5 +79,25 @@ def geo_ftle_grid(spacing=0.2):
 GEO_T0, GEO_T, GEO_PERCENTILE = 180.0, -72.0, 90
 
 
+def geo_batch_specs(seed=1, nfields=48):
+    """The batched time-series workload on the geophysical flow: 48 fields at
+    hourly t0 = 168 + k h, T ~ U[-120, -24] h and grid spacing drawn from
+    {0.1, 0.2, 0.4} deg (1351x501, 676x251 or 338x126 particles), numpy
+    ``default_rng(seed)``.  Returns [(t0, T, spacing)]."""
+    rng = np.random.default_rng(seed)
+    T = rng.uniform(-120.0, -24.0, nfields)
+    sp = rng.choice([0.1, 0.2, 0.4], nfields)
+    return [(168.0 + k, float(T[k]), float(sp[k])) for k in range(nfields)]
+
+
+def bickley_batch_grid(nx=1001, ny=301):
+    """Bickley jet particle grid over its domain (0, pi * 6.371) x (-3, 3) Mm."""
+    return np.linspace(0.0, np.pi * 6.371, nx), np.linspace(-3.0, 3.0, ny)
+
+
+# Bickley jet field of the batch: t0 = 0, T = 40 days, default parameters
+BICKLEY_T0, BICKLEY_T = 0.0, 40.0
+
+
 def double_gyre_grid(nx=401, ny=201):
     return np.linspace(0.0, 2.0, nx), np.linspace(0.0, 1.0, ny)
