@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched time-series leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--rtol", type=float, default=None, help="fixed rtol (skips the accuracy ladder)")
@@ -250,11 +251,17 @@ def run_ours(args, rank, world):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
+    # launch shape (lanes per particle, grid cap) from the autotuner cache
+    from numbacs_gb300.autotune import tune_flowmap
+    lanes, bps = tune_flowmap(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
+                              blocks=(0, 4, 6, 8))
+
     def step(ev=None):
         if ev is not None:
             ev[0].record(stream)
         fm = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
-                                out=fm_buf, return_status=True)[0]
+                                out=fm_buf, return_status=True, lanes_per_particle=lanes,
+                                blocks_per_sm=bps)[0]
         if ev is not None:
             ev[1].record(stream)
         f, e = nb.ftle_evec_2D(fm, T, wl["dx"], wl["dy"])
@@ -342,7 +349,8 @@ def run_ours(args, rank, world):
         "config": {"workload": "geo spline flow 121x217x101, 676x251 particles, t0=180h T=-72h, "
                                "FTLE + ridges p90", "particles": npart, "precision": prec,
                    "rtol": rtol, "atol": atol, "l2": "flushed between timed steps",
-                   "parallelism": "field per GPU" if world > 1 else "single GPU"},
+                   "parallelism": "field per GPU" if world > 1 else "single GPU",
+                   "lanes_per_particle": lanes, "blocks_per_sm": bps},
         "gpu_launches": int(launches),
         "clocks": ck,
         "roofline": {"bound": "fp32" if prec == "mixed" else "fp64", "achieved": achieved,
@@ -360,11 +368,63 @@ def run_ours(args, rank, world):
                         "rtol": sel["fp64"]["rtol"], "speedup_mixed_over_plain": t_plain / ms}
                        if t_plain else None),
     }
+    if not args.quick and not args.no_batch:
+        out["batch"] = run_batch(wl, rtol, max(2, min(args.steps, 5)))
     if not args.no_e2e and not args.quick:
         out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
     if not args.no_cpu_baseline and not args.quick and rank == 0:
         out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value)
     return out
+
+
+def run_batch(wl, rtol, steps):
+    """Batched time series: 48 geophysical fields (t0 = 168 + k h, T ~ U[-120, -24] h,
+    spacing in {0.1, 0.2, 0.4} deg) plus the Bickley jet on 1001 x 301 for 40 days, all
+    in one persistent launch replayed from a CUDA graph; against the same fields
+    launched one flowmap_grid_2D + ftle_evec_2D call at a time."""
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300 import workloads as W
+    from numbacs_gb300.batch import Field, FTLEBatch
+    atol = 1e-2 * rtol
+    fields = []
+    for t0, T, sp in W.geo_batch_specs(seed=1):
+        lonf, latf = W.geo_ftle_grid(sp)
+        fields.append(Field(wl["flow"], t0, T, lonf, latf, np.array([-1.0]), rtol=rtol, atol=atol))
+    bj, pbj, _ = nb.get_predefined_flow("bickley_jet")
+    bx, by = W.bickley_batch_grid()
+    fields.append(Field(bj, W.BICKLEY_T0, W.BICKLEY_T, bx, by, pbj, rtol=rtol, atol=atol))
+    batch = FTLEBatch(fields, precision="mixed", blocks_per_sm=None, graph=True)
+    batch.run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        batch.run()
+    b.record()
+    torch.cuda.synchronize()
+    ms_batch = a.elapsed_time(b) / steps
+
+    def sequential():
+        for f in fields:
+            fm = nb.flowmap_grid_2D(f.flow, f.t0, f.T, f.x, f.y, f.params, rtol=f.rtol,
+                                    atol=f.atol, precision="mixed", out=f.flowmap,
+                                    return_status=True)[0]
+            nb.ftle_evec_2D(fm, f.T, f.dx, f.dy)
+
+    sequential()
+    torch.cuda.synchronize()
+    a.record()
+    sequential()
+    b.record()
+    torch.cuda.synchronize()
+    ms_seq = a.elapsed_time(b)
+    n = batch.particles
+    return {"fields": len(fields), "particles": n, "precision": "mixed", "rtol": rtol,
+            "blocks_per_sm": batch.blocks_per_sm, "ms_per_batch": ms_batch,
+            "particles_per_s": n / (ms_batch * 1e-3), "fields_per_s": len(fields) / (ms_batch * 1e-3),
+            "sequential_ms": ms_seq, "speedup_vs_sequential": ms_seq / ms_batch,
+            "launch": "one persistent integrator launch + one FTLE launch, CUDA graph replay"}
 
 
 def _profile_traffic(prec):
