@@ -73,9 +73,11 @@ typedef struct nbcs_opts {
     int32_t threads_per_block; /* FP64 path: 0 = library default (128) */
     int32_t blocks_per_sm;     /* grid cap in blocks per SM; 0 = one block per particle tile */
     int32_t lanes_per_particle; /* mixed spline path: 1, 2 or 4 lanes share a particle; 0 = auto */
-    int32_t reserved;
+    int32_t step_model_mode;    /* how a step_model proposal h_m meets the controller's h_c:
+                                   0 = h_m, 1 = min(h_m, h_c), 2 = sqrt(h_m h_c) */
     int32_t* stats;        /* optional device (n,3) int32: accepted, rejected, RHS evals */
-    const void* step_model; /* optional learned initial-step model (device), see nbcs_mlp_* */
+    const void* step_model; /* optional learned step-size proposer (device blob, see nbcs_mlp_*);
+                               mixed precision, spline flows */
 } nbcs_opts;
 
 /* Library version / last error message of the calling host thread. */
@@ -201,6 +203,46 @@ int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int
                    const double* y, int32_t ny, double sdd_thresh, double percentile,
                    uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
                    void* scratch, size_t scratch_bytes, void* stream);
+
+/* --------------------------------------------- learned step-size proposer */
+/* No counterpart in the reference.  An 8 -> 64 -> 64 -> 1 ReLU MLP with BF16
+ * weights and FP32 accumulation (tensor cores, mma.sync m16n8k16) that
+ * proposes log h for the next DOP853 step from local flow features
+ * (lon, lat, t, u, v, du/dx, du/dy, dv/dx); the embedded error estimate still
+ * accepts or rejects every step.
+ *   master parameters: float[nbcs_mlp_param_count()] =
+ *     W1[64][8], b1[64], W2[64][64], b2[64], w3[64], b3
+ *   blob (device, nbcs_mlp_blob_bytes(), 16-byte aligned): header of
+ *     feature mean[8], feature 1/std[8], target mean, target std, b3, pad,
+ *     b1[64], b2[64], w3[64] (floats), then W1 bf16[64][16] (inputs padded
+ *     to 16 with zeros) and W2 bf16[64][64].  nbcs_mlp_pack fills everything
+ *     but the normalisation constants, which the caller writes. */
+size_t nbcs_mlp_blob_bytes(void);
+int nbcs_mlp_param_count(void);
+int nbcs_mlp_pack(const float* params, void* blob, void* stream);
+/* predictions (target units) for n feature rows (n, 8) */
+int nbcs_mlp_predict(const void* blob, const float* feats, int64_t n, float* out, void* stream);
+/* gradient (float[param_count], overwritten) of sum_i (net_i - standardised
+ * target_i)^2 / n with respect to the master parameters, and the unscaled
+ * sum of squares in *loss; both device pointers */
+int nbcs_mlp_grad(const void* blob, const float* feats, const float* targets, int64_t n,
+                  float* grad, float* loss, void* stream);
+/* one Adam step (bias-corrected, step >= 1) on the master parameters; if
+ * blob != NULL it is repacked from them */
+int nbcs_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1,
+                  float beta2, float eps, int32_t step, void* blob, void* stream);
+/* Training data: integrate the grid with the mixed-precision plain
+ * controller and, for a sampled fraction of step attempts (a hash of particle
+ * and step, `sample` in [0, 1]), write the features at the step start to
+ * feats (capacity, 8) and the step that would have met the error target,
+ * log(|h| * 0.9 * err^(-1/8)), to targets; *count (device uint64, caller
+ * zeroes it) counts the samples offered, including any beyond capacity.
+ * Spline flows only. */
+int nbcs_flowmap_log_steps(const nbcs_flow* flow, double t0, double T, const double* x,
+                           int32_t nx, const double* y, int32_t ny, const double* params,
+                           int32_t np, double rtol, double atol, float sample, uint32_t seed,
+                           float* feats, float* targets, int64_t capacity,
+                           unsigned long long* count, void* stream);
 
 /* Allocation-free variant of nbcs_ridge_pts.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory -- a

@@ -30,7 +30,7 @@ class NbcsOpts(ctypes.Structure):
     """Mirror of ``struct nbcs_opts``."""
     _fields_ = [("precision", ctypes.c_int32), ("max_steps", ctypes.c_int32),
                 ("threads_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("lanes_per_particle", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("lanes_per_particle", ctypes.c_int32), ("step_model_mode", ctypes.c_int32),
                 ("stats", ctypes.c_void_p), ("step_model", ctypes.c_void_p)]
 
 
@@ -74,6 +74,16 @@ SIGNATURES = {
     "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
                                       _vp, _sz, _vp]),
+    "nbcs_mlp_blob_bytes": (_sz, []),
+    "nbcs_mlp_param_count": (ctypes.c_int, []),
+    "nbcs_mlp_pack": (ctypes.c_int, [_vp, _vp, _vp]),
+    "nbcs_mlp_predict": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
+    "nbcs_mlp_grad": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+    "nbcs_mlp_adam": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_float, _i32, _vp, _vp]),
+    "nbcs_flowmap_log_steps": (ctypes.c_int, [_FP, _d, _d, _vp, _i32, _vp, _i32, _vp, _i32, _d,
+                                              _d, ctypes.c_float, ctypes.c_uint32, _vp, _vp, _i64,
+                                              _vp, _vp]),
     "nbcs_batch_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_batch_prepare": (ctypes.c_int, [_FP, _i32, ctypes.POINTER(NbcsField), _i32, _i32, _vp,
                                           _sz, ctypes.POINTER(NbcsBatch), _vp]),

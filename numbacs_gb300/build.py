@@ -36,6 +36,8 @@ SOURCES = [
     ("probe.cu", []),
     ("batch32.cu", []),
     ("batch64.cu", ["-fmad=false"]),
+    ("mlp_train.cu", []),
+    ("learned.cu", []),
 ]
 
 

@@ -34,10 +34,9 @@ batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
         if ((long long)c >= total) break;
         const int f = batch_find<true>(fields, nfields, (long long)c);
         const DevField& F = fields[f];
-        const long n = (long)F.nx * F.ny;
-        const long p = (long)((long long)c - F.chunk0) * kBatchChunk + lane;
-        if (p >= n) continue;
-        const int i = (int)(p / F.ny), j = (int)(p - (long)i * F.ny);
+        int i, j;
+        if (!batch_particle(F, (long long)c, lane, &i, &j)) continue;  // whole lane group
+        const long p = (long)i * F.ny + j;
         double r0 = 0.0, r1 = 0.0;
         int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
         if (!(F.mask && F.mask[p])) {
@@ -56,23 +55,29 @@ batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
                 st = dop853_solve32(FlowBickley32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj,
                                     &nf);
                 break;
-            default:
-                if (fl.spherical == 1)
-                    st = dop853_solve32(FlowSpline32<1, 1>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv,
-                                        rtol, atol, nmax, kc, &a, &rj, &nf);
-                else if (fl.spherical == 2)
-                    st = dop853_solve32(FlowSpline32<2, 1>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv,
-                                        rtol, atol, nmax, kc, &a, &rj, &nf);
-                else
-                    st = dop853_solve32(FlowSpline32<0, 1>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv,
-                                        rtol, atol, nmax, kc, &a, &rj, &nf);
+            default:  // spline fields run two lanes per particle
+#define NBCS_SPLINE_SOLVE(SPH, LP)                                                              \
+    st = dop853_solve32(FlowSpline32<SPH, LP>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv, rtol,  \
+                        atol, nmax, kc, &a, &rj, &nf)
+                if (F.lp == 2) {
+                    if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 2);
+                    else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 2);
+                    else NBCS_SPLINE_SOLVE(0, 2);
+                } else {
+                    if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 1);
+                    else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 1);
+                    else NBCS_SPLINE_SOLVE(0, 1);
+                }
+#undef NBCS_SPLINE_SOLVE
                 break;
             }
             r0 = f2_to_double(yv[0]);
             r1 = f2_to_double(yv[1]);
         }
-        reinterpret_cast<double2*>(F.out)[p] = make_double2(r0, r1);
-        if (F.status) F.status[p] = st;
+        if ((lane % F.lp) == 0) {
+            reinterpret_cast<double2*>(F.out)[p] = make_double2(r0, r1);
+            if (F.status) F.status[p] = st;
+        }
     }
 }
 
@@ -179,10 +184,12 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         D.status = F.status;
         D.ftle = F.ftle;
         D.evec = F.evec_max;
+        D.lp = (precision == NBCS_PREC_MIXED && flows[F.flow].kind == NBCS_FLOW_SPLINE2D) ? 2 : 1;
         D.chunk0 = chunks;
         D.block0 = blocks;
         long n = (long)F.nx * F.ny;
-        chunks += (n + kBatchChunk - 1) / kBatchChunk;
+        const int tj = batch_tile_j(D.lp);
+        chunks += (long long)((F.nx + kBatchTileI - 1) / kBatchTileI) * ((F.ny + tj - 1) / tj);
         if (F.ftle) blocks += (n + kFtleBlock - 1) / kFtleBlock;
     }
     hdr->counter = 0;

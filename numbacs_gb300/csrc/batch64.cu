@@ -24,10 +24,9 @@ batch64_kernel(BatchHeader* hdr, const DevFlow64* __restrict__ flows,
         if ((long long)c >= total) break;
         const int f = batch_find<true>(fields, nfields, (long long)c);
         const DevField& F = fields[f];
-        const long n = (long)F.nx * F.ny;
-        const long p = (long)((long long)c - F.chunk0) * kBatchChunk + lane;
-        if (p >= n) continue;
-        const int i = (int)(p / F.ny), j = (int)(p - (long)i * F.ny);
+        int i, j;
+        if (!batch_particle(F, (long long)c, lane, &i, &j)) continue;
+        const long p = (long)i * F.ny + j;
         double yv[2] = {0.0, 0.0};
         int st = NBCS_PARTICLE_MASKED;
         Dop853Stats s = {0, 0, 0};

@@ -12,8 +12,13 @@
 
 namespace nbcs {
 
-constexpr int kBatchChunk = 32;        // particles per work unit (one warp, one lane each)
+// A work unit is one warp's worth of particles taken as a 2-D tile of the
+// field's grid: 4 x 8 particles at one lane per particle, 4 x 4 at two lanes
+// per particle (the spline right-hand side of the mixed path).
+constexpr int kBatchTileI = 4;
 constexpr int kBatchThreads = 128;
+
+__host__ __device__ __forceinline__ int batch_tile_j(int lp) { return lp == 1 ? 8 : 4; }
 constexpr int kFtleBlock = 256;        // points per FTLE work unit
 
 struct BatchHeader {
@@ -38,6 +43,7 @@ struct DevFlow64 {
 
 struct DevField {
     int flow, nx, ny, has_ftle;
+    int lp, pad_;  // lanes per particle of this field's work units
     double ts, te, rtol, atol;
     double den, dx, dy;  // FTLE: 2|T| and grid spacing
     Params P;
@@ -79,6 +85,21 @@ __device__ __forceinline__ int batch_find(const DevField* __restrict__ fields, i
         else hi = mid - 1;
     }
     return lo;
+}
+
+// Particle (i, j) of lane `lane` in work unit c of field F; false past the grid edge.
+__device__ __forceinline__ bool batch_particle(const DevField& F, long long c, int lane, int* i,
+                                               int* j)
+{
+    const int lp = F.lp, tj = batch_tile_j(lp);
+    const long r = (long)(c - F.chunk0);
+    const int tiles_j = (F.ny + tj - 1) / tj;
+    const long tI = r / tiles_j;
+    const int tJ = (int)(r - tI * tiles_j);
+    const int p = lane / lp;
+    *i = (int)(tI * kBatchTileI) + p / tj;
+    *j = tJ * tj + p % tj;
+    return *i < F.nx && *j < F.ny;
 }
 
 int launch_batch32(const BatchHeader* dev_hdr, const DevFlow32* flows, const DevField* fields,

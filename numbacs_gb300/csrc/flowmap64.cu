@@ -175,6 +175,13 @@ extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, 
     a.lanes = o.lanes_per_particle;
     a.step_model = o.step_model;
     a.stream = as_stream(stream);
+    if (o.step_model) {
+        if (o.precision != NBCS_PREC_MIXED)
+            return set_error(NBCS_ERR_UNSUPPORTED, "step_model needs precision NBCS_PREC_MIXED");
+        if (o.step_model_mode < 0 || o.step_model_mode > 2)
+            return set_error(NBCS_ERR_INVALID, "step_model_mode must be 0, 1 or 2");
+        return launch_flowmap32_learned(flow, a, o.step_model_mode);
+    }
     if (o.precision == NBCS_PREC_MIXED) return launch_flowmap32(flow, a);
     if (o.precision != NBCS_PREC_FP64) return set_error(NBCS_ERR_INVALID, "unknown precision");
     return launch_flowmap64(flow, a);

@@ -24,6 +24,7 @@ struct FlowmapArgs {
 
 int launch_flowmap64(const nbcs_flow* flow, const FlowmapArgs& a);
 int launch_flowmap32(const nbcs_flow* flow, const FlowmapArgs& a);
+int launch_flowmap32_learned(const nbcs_flow* flow, const FlowmapArgs& a, int mode);
 int launch_rhs32(const nbcs_flow* flow, const Params& P, const double* ty, long n, double* dy,
                  cudaStream_t stream);
 

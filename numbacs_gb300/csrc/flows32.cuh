@@ -208,6 +208,64 @@ __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const flo
     *v = av;
 }
 
+// derivative of the cubic B-spline basis with respect to the cell offset t
+__device__ __forceinline__ void bspline_dw32(float t, float* d)
+{
+    float u = 1.0f - t;
+    d[0] = -0.5f * u * u;
+    d[1] = t * fmaf(1.5f, t, -2.0f);                  // (3t^2 - 4t) / 2
+    d[2] = fmaf(t, fmaf(-1.5f, t, 1.0f), 0.5f);      // (-3t^2 + 2t + 1) / 2
+    d[3] = 0.5f * t * t;
+}
+
+// Value and cell-offset derivatives of the tricubic (u, v): r = {u, v, du/dfx,
+// du/dfy, dv/dfx, dv/dfy}, same group-cooperative split and butterfly as
+// spline_eval_uv32.
+template <int LP>
+__device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
+                                                      const float4* __restrict__ c, int it, int ix,
+                                                      int iy, float ft, const float* wx,
+                                                      const float* wy, const float* dwx,
+                                                      const float* dwy, float* r)
+{
+    const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int rr = 0; rr < 4 / LP; ++rr) {
+        const int a = q + rr * LP;
+        const float wt = bspline_w32_one(ft, a);
+        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy;
+        float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const float4* row = base + (size_t)b * g.sx;
+            float4 p0 = __ldg(row), p1 = __ldg(row + 2);
+            float bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
+            float bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
+            float du = fmaf(dwy[0], p0.x, fmaf(dwy[1], p0.z, fmaf(dwy[2], p1.x, dwy[3] * p1.z)));
+            float dv = fmaf(dwy[0], p0.y, fmaf(dwy[1], p0.w, fmaf(dwy[2], p1.y, dwy[3] * p1.w)));
+            s[0] = fmaf(wx[b], bu, s[0]);
+            s[1] = fmaf(wx[b], bv, s[1]);
+            s[2] = fmaf(dwx[b], bu, s[2]);
+            s[3] = fmaf(wx[b], du, s[3]);
+            s[4] = fmaf(dwx[b], bv, s[4]);
+            s[5] = fmaf(wx[b], dv, s[5]);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[k] = fmaf(wt, s[k], acc[k]);
+    }
+    if (LP > 1) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned gmask = ((1u << LP) - 1u) << (lane & ~(unsigned)(LP - 1));
+#pragma unroll
+        for (int o = 1; o < LP; o <<= 1)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) acc[k] += __shfl_xor_sync(gmask, acc[k], o);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r[k] = acc[k];
+}
+
 template <int SPH, int LP_>
 struct FlowSpline32 {
     static constexpr int LP = LP_;
@@ -244,6 +302,44 @@ struct FlowSpline32 {
             dy[0] = p0 * u;
             dy[1] = p0 * v;
         }
+    }
+
+    // RHS plus its spatial Jacobian J = d(dy)/d(x, y) (row-major 2x2), from
+    // the derivative of the B-spline basis; the metric factor 1/cos(lat) of
+    // the spherical modes is held fixed (its own derivative is left out).
+    // Used for the learned step proposer's features.
+    __device__ __forceinline__ void eval_grad(float th, float ts, const float* yh, const float* ys,
+                                              float* dy, float* J, const ParamsF& P) const
+    {
+        const float p0 = P.v[0];
+        float xh = yh[0];
+        if (SPH == 1 || SPH == 2) {
+            float xv = yh[0] + ys[0];
+            float k = floorf((SPH == 1 ? xv + 180.0f : xv) * (1.0f / 360.0f));
+            if (k != 0.0f) xh = fmaf(-360.0f, k, xh);
+        }
+        float ft, fx, fy, wx[4], wy[4], dwx[4], dwy[4], r[6];
+        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft);
+        int ix = locate_pair(g.ax[1], xh, ys[0], &fx);
+        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy);
+        bspline_w32(fx, wx);
+        bspline_w32(fy, wy);
+        bspline_dw32(fx, dwx);
+        bspline_dw32(fy, dwy);
+        spline_eval_uv32_grad<LP>(g, c, it, ix, iy, ft, wx, wy, dwx, dwy, r);
+        float kx = p0, ky = p0;
+        if (SPH == 1 || SPH == 2) {
+            float lat = yh[1] + ys[1];
+            kx = p0 * deg_per_km / cospif(lat * (1.0f / 180.0f));
+            ky = p0 * deg_per_km;
+        }
+        const float gx = g.ax[1].dinv, gy = g.ax[2].dinv;
+        dy[0] = kx * r[0];
+        dy[1] = ky * r[1];
+        J[0] = kx * r[2] * gx;  // du/dx
+        J[1] = kx * r[3] * gy;  // du/dy
+        J[2] = ky * r[4] * gx;  // dv/dx
+        J[3] = ky * r[5] * gy;  // dv/dy
     }
 };
 

@@ -22,7 +22,8 @@ STATUS_NAMES = {0: "ok", 1: "masked", -2: "max_steps", -3: "step_underflow", -4:
 
 def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, atol=1e-8,
                     mask=None, *, precision="fp64", max_steps=100000, return_status=False,
-                    return_stats=False, out=None, lanes_per_particle=0, blocks_per_sm=0):
+                    return_stats=False, out=None, lanes_per_particle=0, blocks_per_sm=0,
+                    step_model=None, step_model_mode=1):
     """Flow map at t0+T of every particle on the grid x by y -> (nx, ny, 2).
 
     Same positional signature and defaults as the reference.  Keyword-only
@@ -34,7 +35,10 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
     (nx, ny, 2) float64 CUDA tensor), and the launch-shape knobs
     ``lanes_per_particle`` (mixed spline path: 1, 2 or 4 lanes share one
     particle's RHS; 0 = automatic) and ``blocks_per_sm`` (0 = one block per
-    particle tile).
+    particle tile).  ``step_model`` (a learned.StepProposer; mixed precision,
+    spline flows) proposes each step from local flow features, and
+    ``step_model_mode`` combines its proposal h_m with the controller's h_c
+    (0: h_m, 1: min(h_m, h_c), 2: sqrt(h_m h_c)).
 
     ``method="lsoda"`` raises NotImplementedError: only DOP853 runs on the GPU.
     Particles whose integration failed (step limit, step underflow, NaN) keep
@@ -66,6 +70,9 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
     opts.max_steps = int(max_steps)
     opts.lanes_per_particle = int(lanes_per_particle)
     opts.blocks_per_sm = int(blocks_per_sm)
+    if step_model is not None:
+        opts.step_model = step_model.blob.data_ptr()
+        opts.step_model_mode = int(step_model_mode)
     opts.stats = stats.data_ptr() if stats is not None else None
     L = _lib.load()
     _lib.check(L.nbcs_flowmap_grid_2d(flow.struct, float(t0), float(T), D.ptr(xd), nx, D.ptr(yd),

@@ -1,0 +1,90 @@
+"""Learned step-size proposer: tensor-core MLP kernels against the FP64 CPU
+reference, training-data logging, and the proposer inside the integrator."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(n, seed=0):
+    rng = np.random.default_rng(seed)
+    f = rng.standard_normal((n, 8)).astype(np.float32) * np.array(
+        [30, 10, 50, 0.3, 0.2, 0.05, 0.04, 0.03], np.float32) + np.array(
+        [-40, 20, 150, 0, 0, 0, 0, 0], np.float32)
+    t = (np.sin(f[:, 0] / 20) + 0.3 * f[:, 3] - 1.5).astype(np.float32)
+    return f, t
+
+
+def test_mlp_gradient_matches_cpu_reference(nb):
+    from oracle import mlp_ref
+    from numbacs_gb300.learned import StepProposer
+    f, t = _data(1000)
+    sp = StepProposer(seed=3)
+    fd, td = torch.from_numpy(f).cuda(), torch.from_numpy(t).cuda()
+    sp.set_normalization(fd, td)
+    # a few Adam steps so the weights are not at their initial values
+    for _ in range(3):
+        sp.gradient(fd, td)
+        sp.adam_step(1e-2)
+    g, mse = sp.gradient(fd, td)
+    p = sp.params.cpu().numpy().astype(np.float64)
+    mu, isg, omu, osg = sp.consts
+    gref, lref = mlp_ref.loss_grad(p, f, t, mu, isg, omu, osg)
+    g = g.cpu().numpy().astype(np.float64)
+    assert np.isclose(mse * len(t), lref, rtol=1e-4)
+    for name, a, b in [("W1", 0, 512), ("b1", 512, 576), ("W2", 576, 4672), ("b2", 4672, 4736),
+                       ("w3", 4736, 4800), ("b3", 4800, 4801)]:
+        scale = np.abs(gref[a:b]).max()
+        assert np.abs(g[a:b] - gref[a:b]).max() <= 2e-3 * scale + 1e-7, name
+    # predictions
+    pr = sp.predict(fd).cpu().numpy()
+    pref = mlp_ref.predict(p, f, mu, isg, omu, osg)
+    assert np.abs(pr - pref).max() <= 1e-3 * max(1.0, np.abs(pref).max())
+
+
+def test_mlp_training_reduces_loss(nb):
+    from numbacs_gb300.learned import StepProposer
+    f, t = _data(40000, seed=1)
+    fv, tv = _data(4000, seed=2)
+    sp = StepProposer(seed=0)
+    fd, td = torch.from_numpy(f).cuda(), torch.from_numpy(t).cuda()
+    val = (torch.from_numpy(fv).cuda(), torch.from_numpy(tv).cuda())
+    hist = sp.train(fd, td, epochs=6, batch=4096, lr=3e-3, val=val)
+    assert hist[-1]["val_mse"] < 0.2 * hist[0]["val_mse"] or hist[-1]["val_mse"] < 0.05
+
+
+def _geo_flow(nb, seed=0):
+    from numbacs_gb300 import workloads as W
+    t, lon, lat = W.geo_grid()
+    t, lon, lat = t[::4], lon[::4], lat[::4]
+    _, _, _, U, V = W.geo_velocity(seed, t=t, lon=lon, lat=lat, nmodes=64)
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, U, V)
+    return nb.get_flow_2D(grid, Cu, Cv, spherical=1), lon, lat
+
+
+def test_log_steps_and_proposer_keep_accuracy(nb):
+    from numbacs_gb300.learned import StepProposer, log_steps
+    fl, lon, lat = _geo_flow(nb, 0)
+    xf = np.linspace(lon[0], lon[-1], 65)
+    yf = np.linspace(lat[0], lat[-1], 33)
+    p = np.array([-1.0])
+    feats, targ, n = log_steps(fl, 180.0, -72.0, xf, yf, p, sample=1.0, capacity=1 << 20)
+    assert n == feats.shape[0] > 1000
+    assert torch.isfinite(feats).all() and torch.isfinite(targ).all()
+    # logged features: positions inside the sampled window, time within the span
+    assert float(feats[:, 2].min()) >= 108.0 - 1e-3 and float(feats[:, 2].max()) <= 180.0 + 1e-3
+    sp = StepProposer(seed=0)
+    sp.train(feats, targ, epochs=3, batch=8192)
+    truth = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, rtol=1e-12, atol=1e-14)
+    plain, ps, pst = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, precision="mixed",
+                                        return_status=True, return_stats=True, lanes_per_particle=1)
+    for mode in (0, 1, 2):
+        ml, ms, mst = nb.flowmap_grid_2D(fl, 180.0, -72.0, xf, yf, p, precision="mixed",
+                                         return_status=True, return_stats=True, step_model=sp,
+                                         step_model_mode=mode)
+        assert (ms == 0).all(), mode
+        e_ml = np.median(np.abs(ml - truth).max(-1))
+        e_pl = np.median(np.abs(plain - truth).max(-1))
+        # the error estimate still judges every step: same accuracy class
+        assert e_ml <= 5 * e_pl + 1e-7, (mode, e_ml, e_pl)
