@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched time-series leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned step proposer")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--rtol", type=float, default=None, help="fixed rtol (skips the accuracy ladder)")
@@ -222,6 +223,7 @@ def run_ours(args, rank, world):
 
     # precision / rtol selection against an FP64 truth
     sel = {}
+    truth = None
     if args.rtol:
         sel = {"mixed": {"rtol": args.rtol, "ladder": []}, "fp64": {"rtol": args.rtol, "ladder": []}}
     else:
@@ -230,12 +232,40 @@ def run_ours(args, rank, world):
         for p_ in ("mixed", "fp64"):
             r, rows = choose_rtol(nb, wl, x, y, p_, truth)
             sel[p_] = {"rtol": r, "ladder": rows}
-        del truth
     prec = args.precision
     if prec == "auto":
         prec = "mixed" if sel["mixed"]["rtol"] is not None else "fp64"
     rtol = sel[prec]["rtol"] or RTOL_LADDER[-1]
     atol = 1e-2 * rtol
+
+    # learned step proposer: trained on other flows, used for the headline step
+    # only when it is faster at the same accuracy bound
+    proposer, learned = None, None
+    if prec == "mixed" and not args.quick and not args.no_learned:
+        sp, learned = train_proposer(rtol, atol)
+        ms = {}
+        for name, kw in (("mixed", {}), ("mixed+learned", {"step_model": sp, "step_model_mode": 1})):
+            out_ = torch.empty((nx, ny, 2), dtype=torch.float64, device="cuda")
+            nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision="mixed",
+                               out=out_, return_status=True, **kw)
+            a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_.record()
+            for _ in range(3):
+                nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol,
+                                   precision="mixed", out=out_, return_status=True, **kw)
+            b_.record()
+            torch.cuda.synchronize()
+            ms[name] = a_.elapsed_time(b_) / 3
+            if truth is not None:
+                learned["mean_err_" + name] = float((out_ - truth).abs().amax(-1).mean())
+        learned["flowmap_ms"] = ms
+        ok = truth is None or learned["mean_err_mixed+learned"] <= 1e-6 * wl["extent"]
+        if ok and ms["mixed+learned"] < ms["mixed"]:
+            proposer = sp
+        learned["used_for_headline"] = proposer is not None
+        learned["heldout"] = run_learned_eval(sp, rtol, atol)
+    truth = None
+    mkw = {"step_model": proposer, "step_model_mode": 1} if proposer is not None else {}
 
     # algorithmic step counts from the plain FP64 controller at this rtol
     _, _, st64 = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol,
@@ -243,7 +273,7 @@ def run_ours(args, rank, world):
     att = (st64[..., 0] + st64[..., 1]).to(torch.float64)
     flops_launch = float((att * (FLOPS_STEP + 12 * FLOPS_RHS_SPLINE) + 2 * FLOPS_RHS_SPLINE).sum())
     _, _, stp = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
-                                   return_status=True, return_stats=True)
+                                   return_status=True, return_stats=True, **mkw)
     nfcn_mean = float(stp[..., 2].double().mean())
     rej_frac = float(stp[..., 1].sum()) / max(1.0, float((stp[..., 0] + stp[..., 1]).sum()))
 
@@ -261,7 +291,7 @@ def run_ours(args, rank, world):
             ev[0].record(stream)
         fm = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
                                 out=fm_buf, return_status=True, lanes_per_particle=lanes,
-                                blocks_per_sm=bps)[0]
+                                blocks_per_sm=bps, **mkw)[0]
         if ev is not None:
             ev[1].record(stream)
         f, e = nb.ftle_evec_2D(fm, T, wl["dx"], wl["dy"])
@@ -350,7 +380,8 @@ def run_ours(args, rank, world):
                                "FTLE + ridges p90", "particles": npart, "precision": prec,
                    "rtol": rtol, "atol": atol, "l2": "flushed between timed steps",
                    "parallelism": "field per GPU" if world > 1 else "single GPU",
-                   "lanes_per_particle": lanes, "blocks_per_sm": bps},
+                   "lanes_per_particle": lanes, "blocks_per_sm": bps,
+                   "step_proposer": "learned MLP (min with controller)" if proposer else "dop853 controller"},
         "gpu_launches": int(launches),
         "clocks": ck,
         "roofline": {"bound": "fp32" if prec == "mixed" else "fp64", "achieved": achieved,
@@ -359,6 +390,7 @@ def run_ours(args, rank, world):
                      "peak_source": "in-run FMA probe (nbcs_probe_fma), burst",
                      "kernel": "flowmap32_kernel" if prec == "mixed" else "flowmap64_kernel",
                      "flops_per_launch": flops_launch, "launch_ms": fm_ms},
+        "learned": learned,
         "breakdown_ms": {"flowmap": fm_ms, "ftle_evec": sum(t_ftle) / len(t_ftle),
                          "ridge": sum(t_ridge) / len(t_ridge)},
         "accuracy": {"bound": 1e-6 * wl["extent"], "mixed": sel["mixed"], "fp64": sel["fp64"]},
@@ -425,6 +457,97 @@ def run_batch(wl, rtol, steps):
             "particles_per_s": n / (ms_batch * 1e-3), "fields_per_s": len(fields) / (ms_batch * 1e-3),
             "sequential_ms": ms_seq, "speedup_vs_sequential": ms_seq / ms_batch,
             "launch": "one persistent integrator launch + one FTLE launch, CUDA graph replay"}
+
+
+def train_proposer(rtol, atol, seeds=range(8), t0s=(168.0, 190.0, 215.0), sample=0.15):
+    """Step-size MLP trained on steps logged by the integrator on the synthetic
+    geophysical flows of `seeds` (0.4 deg particle grids, T = -72 h)."""
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300 import workloads as W
+    from numbacs_gb300.learned import StepProposer, log_steps
+    t, lon, lat = W.geo_grid()
+    lonf, latf = W.geo_ftle_grid(0.4)
+    F, T = [], []
+    t_log = time.perf_counter()
+    for s in seeds:
+        _, _, _, U, V = W.geo_velocity(s)
+        grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, torch.from_numpy(U).cuda(),
+                                               torch.from_numpy(V).cuda())
+        fl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+        for t0 in t0s:
+            f, tg, _ = log_steps(fl, t0, W.GEO_T, lonf, latf, np.array([-1.0]), rtol=rtol,
+                                 atol=atol, sample=sample, seed=int(s), capacity=1 << 22)
+            F.append(f.clone())
+            T.append(tg.clone())
+    feats, targ = torch.cat(F), torch.cat(T)
+    torch.cuda.synchronize()
+    t_log = time.perf_counter() - t_log
+    n = targ.numel()
+    perm = torch.randperm(n, generator=torch.Generator(device="cuda").manual_seed(0), device="cuda")
+    nval = min(200000, n // 10)
+    val = (feats[perm[:nval]], targ[perm[:nval]])
+    sp = StepProposer(seed=0)
+    t_tr = time.perf_counter()
+    hist = sp.train(feats[perm[nval:]], targ[perm[nval:]], epochs=4, batch=65536, val=val)
+    torch.cuda.synchronize()
+    t_tr = time.perf_counter() - t_tr
+    info = {"samples": int(n), "train_seeds": list(seeds), "log_s": t_log, "train_s": t_tr,
+            "epochs": len(hist), "val_mse_std_units": hist[-1]["val_mse"],
+            "target_std": float(sp.norm[17])}
+    return sp, info
+
+
+def run_learned_eval(sp, rtol, atol, nx_ny=(4001, 2001), t0s=(168.0, 192.0, 216.0, 240.0),
+                     seed=8, mode=1):
+    """Held-out flow (seed 8): plain controller vs the learned proposer on the
+    same GPU -- RHS evaluations, rejected fraction, particles/s and flow-map
+    difference of the learned run from the plain one."""
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300 import workloads as W
+    t, lon, lat = W.geo_grid()
+    _, _, _, U, V = W.geo_velocity(seed)
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, torch.from_numpy(U).cuda(),
+                                           torch.from_numpy(V).cuda())
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    x = torch.linspace(-100.0, 35.0, nx_ny[0], dtype=torch.float64, device="cuda")
+    y = torch.linspace(-5.0, 45.0, nx_ny[1], dtype=torch.float64, device="cuda")
+    p = np.array([-1.0])
+    acc = {"plain": [0.0, 0.0, 0.0, 0.0], "learned": [0.0, 0.0, 0.0, 0.0]}
+    diffs = []
+    for t0 in t0s:
+        res = {}
+        for name, kw in (("plain", {}), ("learned", {"step_model": sp, "step_model_mode": mode})):
+            fm, st, stats = nb.flowmap_grid_2D(fl, t0, W.GEO_T, x, y, p, rtol=rtol, atol=atol,
+                                               precision="mixed", return_status=True,
+                                               return_stats=True, **kw)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            nb.flowmap_grid_2D(fl, t0, W.GEO_T, x, y, p, rtol=rtol, atol=atol, precision="mixed",
+                               return_status=True, out=fm.clone(), **kw)
+            b.record()
+            torch.cuda.synchronize()
+            s = stats.double()
+            acc[name][0] += float(s[..., 2].sum())
+            acc[name][1] += float(s[..., 1].sum())
+            acc[name][2] += float((s[..., 0] + s[..., 1]).sum())
+            acc[name][3] += a.elapsed_time(b)
+            res[name] = fm
+        d = (res["learned"] - res["plain"]).abs().amax(-1).flatten()
+        diffs.append(d)
+    d = torch.cat(diffs).sort().values
+    npart = x.numel() * y.numel() * len(t0s)
+    out = {"grid": list(nx_ny), "t0": list(t0s), "seed": seed, "mode": mode, "rtol": rtol}
+    for name, (nf, rj, att, ms) in acc.items():
+        out[name] = {"rhs_evals_per_particle": nf / npart, "rejected_fraction": rj / att,
+                     "particles_per_s": npart / (ms * 1e-3), "ms_total": ms}
+    out["rhs_eval_reduction"] = 1.0 - out["learned"]["rhs_evals_per_particle"] / \
+        out["plain"]["rhs_evals_per_particle"]
+    out["speedup"] = out["learned"]["particles_per_s"] / out["plain"]["particles_per_s"]
+    out["flowmap_diff_vs_plain_deg"] = {"mean": float(d.mean()), "q99": float(d[int(0.99 * d.numel())]),
+                                        "max": float(d[-1])}
+    return out
 
 
 def _profile_traffic(prec):

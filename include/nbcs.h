@@ -204,6 +204,15 @@ int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int
                    uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
                    void* scratch, size_t scratch_bytes, void* stream);
 
+/* 8-connected component labels of a mask (nx, ny) u8 -> labels (nx, ny)
+ * int32: 0 background, 1..n numbered by each component's first pixel in
+ * row-major order, exactly as scipy.ndimage.label with a 3x3 structure
+ * (the labelling step of ftle_ridges, ridges.py:219-222).  *nlabels (device
+ * int32) receives n, or -1 if the union-find gave up (error flag). */
+size_t nbcs_label8_scratch_bytes(int32_t nx, int32_t ny);
+int nbcs_label8(const uint8_t* mask, int32_t nx, int32_t ny, int32_t* labels, int32_t* nlabels,
+                void* scratch, size_t scratch_bytes, void* stream);
+
 /* --------------------------------------------- learned step-size proposer */
 /* No counterpart in the reference.  An 8 -> 64 -> 64 -> 1 ReLU MLP with BF16
  * weights and FP32 accumulation (tensor cores, mma.sync m16n8k16) that

@@ -38,6 +38,7 @@ SOURCES = [
     ("batch64.cu", ["-fmad=false"]),
     ("mlp_train.cu", []),
     ("learned.cu", []),
+    ("label.cu", []),
 ]
 
 

@@ -239,4 +239,21 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
     return status;
 }
 
+// Thread -> (particle group, lane) map.  A block of kThreads32 threads holds
+// kThreads32/LP particles laid out as a (TI x 8) tile of the grid; tiles run
+// in row-major order.
+template <int LP>
+__device__ __forceinline__ bool tile_particle(long t, int nx, int ny, int* i, int* j)
+{
+    constexpr int PB = kThreads32 / LP, TJ = 8, TI = PB / TJ;
+    long tile = t / kThreads32;
+    int r = (int)(t - tile * kThreads32) / LP;
+    int tiles_j = (ny + TJ - 1) / TJ;
+    long ti = tile / tiles_j;
+    int tj = (int)(tile - ti * tiles_j);
+    *i = (int)(ti * TI) + r / TJ;
+    *j = tj * TJ + (r % TJ);
+    return *i < nx && *j < ny;
+}
+
 }  // namespace nbcs

@@ -170,25 +170,46 @@ __device__ __forceinline__ float bspline_w32_one(float t, int a)
 // Group-cooperative tricubic evaluation.  Coefficients use the "pair" layout:
 // entry k holds (u_k, v_k, u_{k+1}, v_{k+1}) as one float4, so the 4 y taps of
 // a stencil row are two aligned 16-byte loads.
+// Work split of a lane group: with LP >= 2 the two lanes of a pair take the
+// two halves of each 4-tap y row (entries iy and iy + 2 of the pair layout,
+// adjacent 16-byte loads that share a cache line), and with LP = 4 the two
+// pairs take the two halves of the time levels.
+template <int LP>
+struct SplineSplit {
+    static constexpr int kLevels = (LP == 4) ? 2 : 4;  // time levels per lane
+    static constexpr bool kHalfTaps = LP >= 2;
+};
+
 template <int LP>
 __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float4* __restrict__ c,
                                                  int it, int ix, int iy, float ft, const float* wx,
                                                  const float* wy, float* u, float* v)
 {
+    using S = SplineSplit<LP>;
     const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
+    const int tq = S::kHalfTaps ? (q & 1) : 0;    // y-tap half
+    const int a0 = (LP == 4) ? (q >> 1) * 2 : 0;  // first time level
+    const float w0 = wy[2 * tq], w1 = wy[2 * tq + 1];
     float au = 0.0f, av = 0.0f;
 #pragma unroll
-    for (int r = 0; r < 4 / LP; ++r) {
-        const int a = q + r * LP;
+    for (int r = 0; r < S::kLevels; ++r) {
+        const int a = a0 + r;
         const float wt = bspline_w32_one(ft, a);
-        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy;
+        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy + 2 * tq;
         float su = 0.0f, sv = 0.0f;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const float4* row = base + (size_t)b * g.sx;
-            float4 p0 = __ldg(row), p1 = __ldg(row + 2);
-            float bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
-            float bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
+            float bu, bv;
+            if (S::kHalfTaps) {
+                float4 p0 = __ldg(row);
+                bu = fmaf(w0, p0.x, w1 * p0.z);
+                bv = fmaf(w0, p0.y, w1 * p0.w);
+            } else {
+                float4 p0 = __ldg(row), p1 = __ldg(row + 2);
+                bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
+                bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
+            }
             su = fmaf(wx[b], bu, su);
             sv = fmaf(wx[b], bv, sv);
         }
@@ -228,22 +249,34 @@ __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
                                                       const float* wy, const float* dwx,
                                                       const float* dwy, float* r)
 {
+    using S = SplineSplit<LP>;
     const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
+    const int tq = S::kHalfTaps ? (q & 1) : 0;
+    const int a0 = (LP == 4) ? (q >> 1) * 2 : 0;
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int rr = 0; rr < 4 / LP; ++rr) {
-        const int a = q + rr * LP;
+    for (int rr = 0; rr < S::kLevels; ++rr) {
+        const int a = a0 + rr;
         const float wt = bspline_w32_one(ft, a);
-        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy;
+        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy + 2 * tq;
         float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const float4* row = base + (size_t)b * g.sx;
-            float4 p0 = __ldg(row), p1 = __ldg(row + 2);
-            float bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
-            float bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
-            float du = fmaf(dwy[0], p0.x, fmaf(dwy[1], p0.z, fmaf(dwy[2], p1.x, dwy[3] * p1.z)));
-            float dv = fmaf(dwy[0], p0.y, fmaf(dwy[1], p0.w, fmaf(dwy[2], p1.y, dwy[3] * p1.w)));
+            float bu, bv, du, dv;
+            if (S::kHalfTaps) {
+                float4 p0 = __ldg(row);
+                bu = fmaf(wy[2 * tq], p0.x, wy[2 * tq + 1] * p0.z);
+                bv = fmaf(wy[2 * tq], p0.y, wy[2 * tq + 1] * p0.w);
+                du = fmaf(dwy[2 * tq], p0.x, dwy[2 * tq + 1] * p0.z);
+                dv = fmaf(dwy[2 * tq], p0.y, dwy[2 * tq + 1] * p0.w);
+            } else {
+                float4 p0 = __ldg(row), p1 = __ldg(row + 2);
+                bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
+                bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
+                du = fmaf(dwy[0], p0.x, fmaf(dwy[1], p0.z, fmaf(dwy[2], p1.x, dwy[3] * p1.z)));
+                dv = fmaf(dwy[0], p0.y, fmaf(dwy[1], p0.w, fmaf(dwy[2], p1.y, dwy[3] * p1.w)));
+            }
             s[0] = fmaf(wx[b], bu, s[0]);
             s[1] = fmaf(wx[b], bv, s[1]);
             s[2] = fmaf(dwx[b], bu, s[2]);

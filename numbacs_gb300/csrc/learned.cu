@@ -68,7 +68,8 @@ template <class Flow, bool LOG, bool PROPOSE>
 __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2* y, float rtol,
                              float atol, int nmax, float2* kc, bool active, const MlpBlob* W,
                              __nv_bfloat16* xs, float* outs, int mode, const LogSink& sink,
-                             unsigned pid, int* status_out, int* acc, int* rej, int* nfcn)
+                             bool lead, unsigned pid, int* status_out, int* acc, int* rej,
+                             int* nfcn)
 {
     const unsigned FULL = 0xffffffffu;
     const float safe = 0.9f, facc1 = (float)(1.0 / 0.333), facc2 = (float)(1.0 / 6.0);
@@ -200,7 +201,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             continue;
         }
         const float fac11 = nbcs_root8f(err);
-        if (LOG && !last) {  // the clipped last step says nothing about the ideal step
+        if (LOG && lead && !last) {  // the clipped last step says nothing about the ideal step
             const unsigned hv = hash32(pid ^ sink.seed, (unsigned)nstep);
             if ((float)(hv >> 8) * (1.0f / 16777216.0f) < sink.sample) {
                 unsigned long long k = atomicAdd(sink.count, 1ull);
@@ -261,22 +262,19 @@ learned_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restric
     // uniform trip count: nthreads is a multiple of the block size
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nthreads;
          t += (long)gridDim.x * blockDim.x) {
-        // 16x8 particle tiles, as in flowmap32_kernel with one lane per particle
-        const long tile = t >> 7;
-        const int r = (int)(t & 127);
-        const int tiles_j = (ny + 7) / 8;
-        const long ti = tile / tiles_j;
-        const int i = (int)(ti * 16) + (r >> 3), j = (int)(tile - ti * tiles_j) * 8 + (r & 7);
-        const bool valid = i < nx && j < ny;
+        constexpr int LP = Flow::LP;  // lanes of a group hold the same particle
+        int i, j;
+        const bool valid = tile_particle<LP>(t, nx, ny, &i, &j);
+        const bool lead = (threadIdx.x & (LP - 1)) == 0;
         const long k = valid ? (long)i * ny + j : 0;
         const bool live = valid && !(mask && mask[k]);
         F2 yv[2] = {f2_from_double(valid ? x[i] : 0.0), f2_from_double(valid ? y[j] : 0.0)};
         int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
         solve32_warp<Flow, LOG, PROPOSE>(fl, P, xs0, xe, yv, rtol, atol, nmax, kc, live, &W,
-                                         xs[warp], outs[warp], mode, sink, (unsigned)k, &st, &a,
-                                         &rj, &nf);
+                                         xs[warp], outs[warp], mode, sink, lead, (unsigned)k, &st,
+                                         &a, &rj, &nf);
         if (!live) st = NBCS_PARTICLE_MASKED;
-        if (valid) {
+        if (valid && lead) {
             double2 res = live ? make_double2(f2_to_double(yv[0]), f2_to_double(yv[1]))
                                : make_double2(0.0, 0.0);
             if (out) reinterpret_cast<double2*>(out)[k] = res;
@@ -306,15 +304,17 @@ static int launch_learned(const nbcs_flow* flow, const FlowmapArgs& a, const Mlp
     SplineGridF g = make_grid_f(flow->grid);
     const float4* c = reinterpret_cast<const float4*>(flow->coef_uv32);
     float kd = (float)(180.0 / (3.141592653589793 * flow->r));
-    long tiles = (long)((a.nx + 15) / 16) * ((a.ny + 7) / 8);
+    // two lanes per particle (8 x 8 particle tiles per 128-thread block)
+    constexpr int LPL = 2, TI = kThreads32 / LPL / 8;
+    long tiles = (long)((a.nx + TI - 1) / TI) * ((a.ny + 7) / 8);
     long nthreads = tiles * kThreads32;
     long blocks = tiles;
     if (a.blocks_per_sm > 0 && blocks > (long)sm_count() * a.blocks_per_sm)
         blocks = (long)sm_count() * a.blocks_per_sm;
     ParamsF P = to_float_p(a.P);
 #define NBCS_LAUNCH_LEARNED(SPH)                                                              \
-    learned_kernel<FlowSpline32<SPH, 1>, LOG, PROPOSE><<<(unsigned)blocks, kThreads32, 0, a.stream>>>( \
-        FlowSpline32<SPH, 1>{g, c, kd}, P, a.ts, a.te, a.x, a.y, a.nx, a.ny, a.mask, a.out,    \
+    learned_kernel<FlowSpline32<SPH, LPL>, LOG, PROPOSE><<<(unsigned)blocks, kThreads32, 0, a.stream>>>( \
+        FlowSpline32<SPH, LPL>{g, c, kd}, P, a.ts, a.te, a.x, a.y, a.nx, a.ny, a.mask, a.out,    \
         a.status, a.stats, (float)a.rtol, (float)a.atol, a.nmax, nthreads, W, mode, sink)
     switch (flow->spherical) {
     case 1: NBCS_LAUNCH_LEARNED(1); break;

@@ -52,28 +52,49 @@ def _ftle_ridges(f, eigvec_max, x, y, sdd_thresh=0.0, percentile=0):
     return D.finish(full, as_torch), D.finish(mask.to(torch.bool), as_torch), nx, ny
 
 
+def label8(mask):
+    """8-connected component labels of a (nx, ny) mask on the GPU, numbered
+    1..n by first pixel in row-major order (scipy.ndimage.label with a 3x3
+    structure).  Returns (labels int32 CUDA tensor, n)."""
+    D.require_cuda()
+    m = D.mask_to_dev(mask)
+    nx, ny = m.shape
+    L = _lib.load()
+    nbytes = L.nbcs_label8_scratch_bytes(nx, ny)
+    scratch = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=m.device)
+    labels = D.empty((nx, ny), torch.int32)
+    n = D.empty((1,), torch.int32)
+    _lib.check(L.nbcs_label8(D.ptr(m), nx, ny, D.ptr(labels), D.ptr(n), D.ptr(scratch), nbytes,
+                             D.stream_ptr()))
+    k = int(n.item())
+    if k < 0:
+        raise RuntimeError("label8: union-find did not converge")
+    return labels, k
+
+
 def ftle_ridges(f, eigvec_max, x, y, sdd_thresh=0.0, percentile=0, min_ridge_pts=3):
     """Connected ridges: list of (m, 2) point arrays, one per 8-connected
     component of the ridge mask with at least ``min_ridge_pts`` points,
-    components ordered by their first grid point in row-major order
-    (ridges.py:186-229; scipy.ndimage.label with a full 3x3 structure).
+    components ordered by their first grid point in row-major order and
+    points within a ridge in row-major order (ridges.py:186-229).
 
-    The mask and ridge points come from the GPU; the component labelling of
-    the (small, sparse) mask is done with scipy.ndimage.label on the host, as
-    in the reference.
+    Mask, ridge points and component labels are computed on the GPU
+    (csrc/ridges.cu, csrc/label.cu); the per-ridge split of the labelled
+    points is a stable sort by label of the (few) ridge pixels.
     """
-    from scipy.ndimage import generate_binary_structure, label
-
     as_torch = D.is_torch(f, eigvec_max)
-    r_pts, ridge_bool, nx, ny = _ftle_ridges(f, eigvec_max, x, y, sdd_thresh, percentile)
-    rb = ridge_bool.cpu().numpy() if isinstance(ridge_bool, torch.Tensor) else ridge_bool
-    rp = r_pts.cpu().numpy() if isinstance(r_pts, torch.Tensor) else r_pts
-    labels, nlabels = label(rb, structure=generate_binary_structure(2, 2))
-    ind_arr = np.arange(nx * ny).reshape(nx, ny)
-    ridges = []
-    for i in range(1, nlabels + 1):
-        inds = ind_arr[labels == i]
-        if len(inds) >= min_ridge_pts:
-            r = rp[inds, :]
-            ridges.append(torch.from_numpy(r).to(D.device()) if as_torch else r)
+    _, _, mask, full = _run(f, eigvec_max, x, y, sdd_thresh, percentile, True, True)
+    labels, n = label8(mask)
+    lab = labels.view(-1)
+    idx = torch.nonzero(lab, as_tuple=True)[0]  # ascending: row-major
+    labs = lab.index_select(0, idx).long()
+    order = torch.sort(labs, stable=True).indices
+    pts = full.index_select(0, idx.index_select(0, order))
+    counts = torch.bincount(labs, minlength=n + 1)[1:].tolist()
+    ridges, start = [], 0
+    for c in counts:
+        if c >= min_ridge_pts:
+            r = pts[start:start + c]
+            ridges.append(r if as_torch else r.cpu().numpy())
+        start += c
     return ridges

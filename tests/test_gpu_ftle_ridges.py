@@ -147,3 +147,50 @@ def test_ridge_compaction_large(nb):
     assert pts.shape[0] == int(rb.sum())
     assert torch.equal(pts, full[rb.reshape(-1)])
     assert pts.shape[0] > 1000
+
+
+@pytest.mark.parametrize("shape,density,seed", [((1, 1), 1.0, 0), ((7, 5), 0.5, 1),
+                                                ((64, 33), 0.3, 2), ((301, 157), 0.12, 3),
+                                                ((1000, 1000), 0.45, 4), ((4096, 3), 0.7, 5)])
+def test_label8_matches_scipy(nb, shape, density, seed):
+    from scipy.ndimage import generate_binary_structure, label
+    from numbacs_gb300.extraction.ridges import label8
+    m = np.random.default_rng(seed).random(shape) < density
+    lab, n = label8(m)
+    ref, nref = label(m, structure=generate_binary_structure(2, 2))
+    assert n == nref
+    assert np.array_equal(lab.cpu().numpy(), ref)
+    # a spiral: one long component, worst case for path lengths
+    s = np.zeros((64, 64), bool)
+    s[0, :] = s[:, -1] = s[-1, 1:] = s[2:, 0] = s[2, :-2] = True
+    lab, n = label8(s)
+    assert n == nref_spiral(s) and np.array_equal(lab.cpu().numpy(), label(s, np.ones((3, 3)))[0])
+
+
+def nref_spiral(s):
+    from scipy.ndimage import label
+    return label(s, np.ones((3, 3)))[1]
+
+
+def test_ridges_large_field_groups(nb):
+    # ridge grouping at a realistic size vs scipy on the GPU mask
+    from scipy.ndimage import generate_binary_structure, label
+    nx, ny = 676, 251
+    x, y, fm = _ridge_field(nx, ny, seed=3)
+    dx, dy = x[1] - x[0], y[1] - y[0]
+    oev, ovec = orc_like_eig(fm, dx, dy)
+    f = np.where(oev[..., 1] > 1, np.log(np.maximum(oev[..., 1], 1e-300)) / 10.0, 0.0)
+    e = np.ascontiguousarray(ovec[..., :, 1])
+    r_pts, rb, _, _ = nb.extraction._ftle_ridges(f, e, x, y, 0.0, 50)
+    ridges = nb.ftle_ridges(f, e, x, y, 0.0, 50, min_ridge_pts=3)
+    lab, nl = label(rb, structure=generate_binary_structure(2, 2))
+    ind = np.arange(nx * ny).reshape(nx, ny)
+    ref = [r_pts[ind[lab == k]] for k in range(1, nl + 1) if (lab == k).sum() >= 3]
+    assert len(ridges) == len(ref) > 3
+    for a, b in zip(ridges, ref):
+        assert np.array_equal(a, b)
+
+
+def orc_like_eig(fm, dx, dy):
+    import oracle
+    return oracle.C_eig_2D(fm, dx, dy)
