@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched time-series leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned step proposer")
+    ap.add_argument("--sweep", action="store_true",
+                    help="precision sweep (double gyre / geo 0.05 deg, rtol 1e-5..1e-8) only")
+    ap.add_argument("--learned-full", action="store_true",
+                    help="learned proposer: train on seeds 0-7, evaluate seed 8 at 4001x2001 x 96 t0")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--rtol", type=float, default=None, help="fixed rtol (skips the accuracy ladder)")
@@ -550,6 +554,74 @@ def run_learned_eval(sp, rtol, atol, nx_ny=(4001, 2001), t0s=(168.0, 192.0, 216.
     return out
 
 
+def run_sweep(oracle_budget_s=60.0):
+    """Precision sweep: double gyre 2001x1001 and 4001x2001 (T = -10) and the
+    geophysical flow at 0.05 deg (2701x1001, T = -72 h), rtol in {1e-5, 1e-6,
+    1e-8} (atol = 1e-2 rtol): the mixed path against the all-FP64 GPU path and
+    the CPU FP64 oracle (the oracle on every k-th row, all host threads, within
+    a time budget).  Per field: max and mean |mixed - fp64|, |fp64 - oracle|,
+    step counts and times."""
+    import torch
+    import numbacs_gb300 as nb
+    import oracle
+    from numbacs_gb300 import workloads as W
+    oracle.build()
+    rows = []
+    cases = []
+    dg, pdg, _ = nb.get_predefined_flow("double_gyre", int_direction=-1.0)
+    for nx, ny in ((2001, 1001), (4001, 2001)):
+        x, y = W.double_gyre_grid(nx, ny)
+        cases.append(("double_gyre %dx%d" % (nx, ny), dg, oracle.double_gyre(), 0.0, -10.0, x, y,
+                      pdg, 2.0))
+    wl = geo_setup(180.0)
+    lonf, latf = W.geo_ftle_grid(0.05)
+    lonf = lonf[lonf <= 35.0 + 1e-9]
+    cases.append(("geo 0.05deg %dx%d" % (len(lonf), len(latf)), wl["flow"],
+                  oracle.spline_flow(wl["grid"], wl["Cu"], wl["Cv"], spherical=1), 180.0, -72.0,
+                  lonf, latf, np.array([-1.0]), wl["extent"]))
+    for name, fl, ofl, t0, T, x, y, p, extent in cases:
+        xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+        for rtol in (1e-5, 1e-6, 1e-8):
+            atol = 1e-2 * rtol
+            res = {}
+            for prec in ("mixed", "fp64"):
+                fm, st, stats = nb.flowmap_grid_2D(fl, t0, T, xd, yd, p, rtol=rtol, atol=atol,
+                                                   precision=prec, return_status=True,
+                                                   return_stats=True)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                nb.flowmap_grid_2D(fl, t0, T, xd, yd, p, rtol=rtol, atol=atol, precision=prec,
+                                   return_status=True, out=fm.clone())
+                b.record()
+                torch.cuda.synchronize()
+                res[prec] = (fm, st, stats, a.elapsed_time(b))
+            d = (res["mixed"][0] - res["fp64"][0]).abs().amax(-1)
+            row = {"field": name, "rtol": rtol, "particles": len(x) * len(y),
+                   "mixed_vs_fp64_max": float(d.max()), "mixed_vs_fp64_mean": float(d.mean()),
+                   "extent": extent, "mixed_ms": res["mixed"][3], "fp64_ms": res["fp64"][3],
+                   "mixed_steps": float(res["mixed"][2][..., 0:2].sum(-1).double().mean()),
+                   "fp64_steps": float(res["fp64"][2][..., 0:2].sum(-1).double().mean()),
+                   "mixed_status_ok": float((res["mixed"][1] == 0).double().mean()),
+                   "fp64_status_ok": float((res["fp64"][1] == 0).double().mean())}
+            # CPU FP64 oracle on a row sample sized to the budget
+            stride = max(1, int(len(x) / max(1.0, oracle_budget_s * 8000.0 / len(y))))
+            xs = x[::stride]
+            t_o = time.perf_counter()
+            ofm = oracle.flowmap_grid_2D(ofl, t0, T, xs, y, p, rtol=rtol, atol=atol,
+                                         nthreads=os.cpu_count() or 1)
+            t_o = time.perf_counter() - t_o
+            g = res["fp64"][0][::stride].cpu().numpy()
+            m = res["mixed"][0][::stride].cpu().numpy()
+            eo = np.abs(g - ofm).max(-1)
+            em = np.abs(m - ofm).max(-1)
+            row.update({"oracle_rows_every": stride, "oracle_s": t_o,
+                        "fp64_vs_oracle_max": float(eo.max()), "fp64_vs_oracle_mean": float(eo.mean()),
+                        "mixed_vs_oracle_max": float(em.max()), "mixed_vs_oracle_mean": float(em.mean())})
+            rows.append(row)
+            del res
+    return rows
+
+
 def _profile_traffic(prec):
     """DRAM bytes per launch of the integrator from the committed ncu summary."""
     name = "flowmap32_geo.md" if prec == "mixed" else "flowmap64_geo.md"
@@ -687,6 +759,18 @@ def main():
         if rank != 0:
             return 0
         print(json.dumps(run_reference(args, 0, int(os.environ.get("WORLD_SIZE", "1")))))
+        return 0
+    if args.sweep:
+        dist_setup()
+        print(json.dumps({"precision_sweep": run_sweep()}))
+        return 0
+    if args.learned_full:
+        dist_setup()
+        wl_rtol = args.rtol or 1e-7
+        sp, info = train_proposer(wl_rtol, 1e-2 * wl_rtol)
+        t0s = tuple(168.0 + k for k in range(96))
+        info["heldout"] = run_learned_eval(sp, wl_rtol, 1e-2 * wl_rtol, t0s=t0s)
+        print(json.dumps({"learned_full": info}))
         return 0
     rank, world, _ = dist_setup()
     out = run_ours(args, rank, world)

@@ -9,7 +9,7 @@
 //
 // Kernels: init (parent = self or -1), merge (each foreground pixel unites
 // with its W, NW, N, NE neighbours, which covers every 8-adjacency once),
-// flatten (parent = root), root flags + per-block counts, block scan, root
+// flatten (parent = root, read-only walk), root flags + per-block counts, block scan, root
 // numbers, and labels of the non-root pixels.  Every loop is bounded: find()
 // follows parent links that strictly decrease, and unite() gives up (setting
 // an error flag) after a fixed number of failed swaps.
@@ -72,10 +72,19 @@ __global__ void ccl_merge_kernel(int nx, int ny, int* parent, int* err)
     }
 }
 
+// After merging the roots no longer change, so a plain walk up the links finds
+// them.  Flatten must not halve paths: a halving write racing with another
+// thread's final `parent[x] = root` could put a non-root ancestor back.
+__device__ __forceinline__ int ccl_root(const int* parent, int x)
+{
+    for (int p = parent[x]; p != x; p = parent[x]) x = p;
+    return x;
+}
+
 __global__ void ccl_flatten_kernel(long n, int* parent)
 {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
-        if (parent[k] >= 0) parent[k] = ccl_find(parent, (int)k);
+        if (parent[k] >= 0) parent[k] = ccl_root(parent, (int)k);
 }
 
 // one block per kLblThreads pixels: count the roots
