@@ -61,8 +61,9 @@ typedef struct nbcs_flow {
     double r;          /* SPLINE2D spherical: radius (km) for km/h -> deg/h */
     double grid[9];    /* SPLINE2D: t0,t1,nt, x0,x1,nx, y0,y1,ny (UCGrid tuple) */
     const double* coef_uv;  /* SPLINE2D FP64 coefficients (device), required */
-    /* SPLINE2D FP32 copy (device), required for NBCS_PREC_MIXED, in the "pair"
-     * layout: entry k (16 bytes) holds u_k, v_k, u_{k+1}, v_{k+1}; n entries. */
+    /* SPLINE2D FP32 copy (device), required for NBCS_PREC_MIXED, in the "quad"
+     * layout: entry k (32 bytes) holds u_j, v_j for j = k .. k+3 (zeros past the
+     * end); n entries, 32-byte aligned. */
     const float* coef_uv32;
 } nbcs_flow;
 
@@ -95,7 +96,8 @@ int nbcs_spline_prefilter_3d(const double* f, int32_t nt, int32_t nx, int32_t ny
 
 /* get_flow_2D coefficient capture (flows.py:156-254 closes over C_eval_u /
  * C_eval_v): interleave cu, cv (n nodes each) into coef_uv (2n doubles) and,
- * if coef_uv32 != NULL, an FP32 copy in the pair layout (4n floats). */
+ * if coef_uv32 != NULL, an FP32 copy in the quad layout (8n floats, 32-byte
+ * aligned; coef_uv 16-byte aligned). */
 int nbcs_spline_pack_uv(const double* cu, const double* cv, int64_t n, double* coef_uv,
                         float* coef_uv32, void* stream);
 

@@ -144,7 +144,7 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
             f32[k].g = make_grid_f(fl.grid);
             f64[k].g = make_grid(fl.grid);
         }
-        f32[k].c = reinterpret_cast<const float4*>(fl.coef_uv32);
+        f32[k].c = fl.coef_uv32;
         f64[k].c = reinterpret_cast<const double2*>(fl.coef_uv);
         f32[k].deg_per_km = (float)(180.0 / (3.141592653589793 * fl.r));
         f64[k].r = fl.r;

@@ -30,7 +30,7 @@ struct BatchHeader {
 struct DevFlow32 {
     int kind, spherical;
     SplineGridF g;
-    const float4* c;
+    const float* c;  // quad layout
     float deg_per_km;
 };
 

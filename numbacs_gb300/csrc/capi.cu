@@ -60,6 +60,8 @@ int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int p
         if (!flow->coef_uv) return set_error(NBCS_ERR_INVALID, "spline flow without coefficients");
         if (precision == NBCS_PREC_MIXED && !flow->coef_uv32)
             return set_error(NBCS_ERR_INVALID, "mixed precision needs the FP32 coefficient copy");
+        if (precision == NBCS_PREC_MIXED && (reinterpret_cast<uintptr_t>(flow->coef_uv32) & 31))
+            return set_error(NBCS_ERR_INVALID, "the FP32 coefficient copy must be 32-byte aligned");
         break;
     }
     default:

@@ -88,7 +88,7 @@ static ParamsF to_float(const Params& P)
 }
 
 template <int SPH, class F>
-static int dispatch_lp(int lp, const SplineGridF& g, const float4* c, float k, const F& f)
+static int dispatch_lp(int lp, const SplineGridF& g, const float* c, float k, const F& f)
 {
     switch (lp) {
     case 1: return f(FlowSpline32<SPH, 1>{g, c, k});
@@ -115,7 +115,7 @@ static int dispatch32(const nbcs_flow* flow, int lp, const F& f)
     case NBCS_FLOW_BICKLEY: return f(FlowBickley32{});
     default: {
         SplineGridF g = make_grid_f(flow->grid);
-        const float4* c = reinterpret_cast<const float4*>(flow->coef_uv32);
+        const float* c = flow->coef_uv32;
         float k = (float)(180.0 / (3.141592653589793 * flow->r));
         switch (flow->spherical) {
         case 1: return dispatch_lp<1>(lp, g, c, k, f);

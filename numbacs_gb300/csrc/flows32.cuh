@@ -14,8 +14,8 @@
 // the unstable direction).
 //
 // The spline RHS can be evaluated cooperatively by a group of LP = 1, 2 or 4
-// adjacent lanes that hold the same particle: lane q of the group sums the
-// time levels q, q + LP, ... of the 4x4x4 stencil and a butterfly of
+// adjacent lanes that hold the same particle: lane q of the group sums 4/LP of
+// the time levels of the 4x4x4 stencil and a butterfly of
 // __shfl_xor_sync adds the partial sums, so every lane of the group ends with
 // bit-identical velocities (float addition is commutative).
 #pragma once
@@ -167,49 +167,49 @@ __device__ __forceinline__ float bspline_w32_one(float t, int a)
     }
 }
 
-// Group-cooperative tricubic evaluation.  Coefficients use the "pair" layout:
-// entry k holds (u_k, v_k, u_{k+1}, v_{k+1}) as one float4, so the 4 y taps of
-// a stencil row are two aligned 16-byte loads.
-// Work split of a lane group: with LP >= 2 the two lanes of a pair take the
-// two halves of each 4-tap y row (entries iy and iy + 2 of the pair layout,
-// adjacent 16-byte loads that share a cache line), and with LP = 4 the two
-// pairs take the two halves of the time levels.
+// Group-cooperative tricubic evaluation.  Coefficients use the "quad" layout:
+// entry k (32 bytes, 32-byte aligned) holds (u_j, v_j) for j = k .. k+3, so the
+// 4 y taps of a stencil row are ONE 256-bit load (ld.global.nc.v8.f32).  The
+// gathers are what bounds this kernel (the L1 data stage, not DRAM: the
+// coefficients stay in L2), and one aligned 32-byte sector per row costs half
+// the L1 wavefronts of two 16-byte loads.
+// Work split of a lane group: lane q takes time levels q*4/LP .. (q+1)*4/LP - 1.
 template <int LP>
 struct SplineSplit {
-    static constexpr int kLevels = (LP == 4) ? 2 : 4;  // time levels per lane
-    static constexpr bool kHalfTaps = LP >= 2;
+    static constexpr int kLevels = 4 / LP;  // time levels per lane
+    __device__ static int first_level(int q) { return q * kLevels; }
 };
 
+// one stencil row: taps iy .. iy+3 of (u, v) from a quad entry
+__device__ __forceinline__ void ldg_row8(const float* __restrict__ p, float* r)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]),
+          "=f"(r[7])
+        : "l"(p));
+}
+
 template <int LP>
-__device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float4* __restrict__ c,
+__device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float* __restrict__ c,
                                                  int it, int ix, int iy, float ft, const float* wx,
                                                  const float* wy, float* u, float* v)
 {
     using S = SplineSplit<LP>;
     const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
-    const int tq = S::kHalfTaps ? (q & 1) : 0;    // y-tap half
-    const int a0 = (LP == 4) ? (q >> 1) * 2 : 0;  // first time level
-    const float w0 = wy[2 * tq], w1 = wy[2 * tq + 1];
+    const int a0 = S::first_level(q);  // first time level
     float au = 0.0f, av = 0.0f;
 #pragma unroll
     for (int r = 0; r < S::kLevels; ++r) {
         const int a = a0 + r;
         const float wt = bspline_w32_one(ft, a);
-        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy + 2 * tq;
+        const float* base = c + 8 * ((size_t)(it + a) * g.st + (size_t)ix * g.sx + iy);
         float su = 0.0f, sv = 0.0f;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float4* row = base + (size_t)b * g.sx;
-            float bu, bv;
-            if (S::kHalfTaps) {
-                float4 p0 = __ldg(row);
-                bu = fmaf(w0, p0.x, w1 * p0.z);
-                bv = fmaf(w0, p0.y, w1 * p0.w);
-            } else {
-                float4 p0 = __ldg(row), p1 = __ldg(row + 2);
-                bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
-                bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
-            }
+            float p[8];
+            ldg_row8(base + 8 * (size_t)b * g.sx, p);
+            const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
+            const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
             su = fmaf(wx[b], bu, su);
             sv = fmaf(wx[b], bv, sv);
         }
@@ -244,39 +244,29 @@ __device__ __forceinline__ void bspline_dw32(float t, float* d)
 // spline_eval_uv32.
 template <int LP>
 __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
-                                                      const float4* __restrict__ c, int it, int ix,
+                                                      const float* __restrict__ c, int it, int ix,
                                                       int iy, float ft, const float* wx,
                                                       const float* wy, const float* dwx,
                                                       const float* dwy, float* r)
 {
     using S = SplineSplit<LP>;
     const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
-    const int tq = S::kHalfTaps ? (q & 1) : 0;
-    const int a0 = (LP == 4) ? (q >> 1) * 2 : 0;
+    const int a0 = S::first_level(q);
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int rr = 0; rr < S::kLevels; ++rr) {
         const int a = a0 + rr;
         const float wt = bspline_w32_one(ft, a);
-        const float4* base = c + (size_t)(it + a) * g.st + (size_t)ix * g.sx + iy + 2 * tq;
+        const float* base = c + 8 * ((size_t)(it + a) * g.st + (size_t)ix * g.sx + iy);
         float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float4* row = base + (size_t)b * g.sx;
-            float bu, bv, du, dv;
-            if (S::kHalfTaps) {
-                float4 p0 = __ldg(row);
-                bu = fmaf(wy[2 * tq], p0.x, wy[2 * tq + 1] * p0.z);
-                bv = fmaf(wy[2 * tq], p0.y, wy[2 * tq + 1] * p0.w);
-                du = fmaf(dwy[2 * tq], p0.x, dwy[2 * tq + 1] * p0.z);
-                dv = fmaf(dwy[2 * tq], p0.y, dwy[2 * tq + 1] * p0.w);
-            } else {
-                float4 p0 = __ldg(row), p1 = __ldg(row + 2);
-                bu = fmaf(wy[0], p0.x, fmaf(wy[1], p0.z, fmaf(wy[2], p1.x, wy[3] * p1.z)));
-                bv = fmaf(wy[0], p0.y, fmaf(wy[1], p0.w, fmaf(wy[2], p1.y, wy[3] * p1.w)));
-                du = fmaf(dwy[0], p0.x, fmaf(dwy[1], p0.z, fmaf(dwy[2], p1.x, dwy[3] * p1.z)));
-                dv = fmaf(dwy[0], p0.y, fmaf(dwy[1], p0.w, fmaf(dwy[2], p1.y, dwy[3] * p1.w)));
-            }
+            float p[8];
+            ldg_row8(base + 8 * (size_t)b * g.sx, p);
+            const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
+            const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
+            const float du = fmaf(dwy[0], p[0], fmaf(dwy[1], p[2], fmaf(dwy[2], p[4], dwy[3] * p[6])));
+            const float dv = fmaf(dwy[0], p[1], fmaf(dwy[1], p[3], fmaf(dwy[2], p[5], dwy[3] * p[7])));
             s[0] = fmaf(wx[b], bu, s[0]);
             s[1] = fmaf(wx[b], bv, s[1]);
             s[2] = fmaf(dwx[b], bu, s[2]);
@@ -303,7 +293,7 @@ template <int SPH, int LP_>
 struct FlowSpline32 {
     static constexpr int LP = LP_;
     SplineGridF g;
-    const float4* __restrict__ c;
+    const float* __restrict__ c;  // quad layout, 32-byte aligned
     float deg_per_km;  // 180 / (pi r)
 
     __device__ __forceinline__ void operator()(float th, float ts, const float* yh, const float* ys,

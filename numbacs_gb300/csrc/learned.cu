@@ -302,7 +302,7 @@ static int launch_learned(const nbcs_flow* flow, const FlowmapArgs& a, const Mlp
     if (flow->kind != NBCS_FLOW_SPLINE2D)
         return set_error(NBCS_ERR_UNSUPPORTED, "the learned step proposer needs a spline flow");
     SplineGridF g = make_grid_f(flow->grid);
-    const float4* c = reinterpret_cast<const float4*>(flow->coef_uv32);
+    const float* c = flow->coef_uv32;
     float kd = (float)(180.0 / (3.141592653589793 * flow->r));
     // two lanes per particle (8 x 8 particle tiles per 128-thread block)
     constexpr int LPL = 2, TI = kThreads32 / LPL / 8;

@@ -75,8 +75,9 @@ __global__ void prefilter_lines_kernel(const double* __restrict__ f, double* __r
     }
 }
 
-// FP64 (u, v) per node, and the FP32 "pair" layout: entry k = (u_k, v_k,
-// u_{k+1}, v_{k+1}) so a 4-tap stencil row is two aligned 16-byte loads.
+// FP64 (u, v) per node, and the FP32 "quad" layout: entry k = (u_j, v_j) for
+// j = k .. k+3 (32 bytes; zeros past the end) so a 4-tap stencil row is one
+// aligned 32-byte load.
 __global__ void pack_uv_kernel(const double* __restrict__ cu, const double* __restrict__ cv, long n,
                                double2* __restrict__ uv, float4* __restrict__ uv32)
 {
@@ -85,12 +86,14 @@ __global__ void pack_uv_kernel(const double* __restrict__ cu, const double* __re
         double u = cu[k], v = cv[k];
         uv[k] = make_double2(u, v);
         if (uv32) {
-            float u1 = 0.f, v1 = 0.f;
-            if (k + 1 < n) {
-                u1 = (float)cu[k + 1];
-                v1 = (float)cv[k + 1];
+            float q[8];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                q[2 * j] = k + j < n ? (float)cu[k + j] : 0.f;
+                q[2 * j + 1] = k + j < n ? (float)cv[k + j] : 0.f;
             }
-            uv32[k] = make_float4((float)u, (float)v, u1, v1);
+            uv32[2 * k] = make_float4(q[0], q[1], q[2], q[3]);
+            uv32[2 * k + 1] = make_float4(q[4], q[5], q[6], q[7]);
         }
     }
 }
@@ -154,8 +157,9 @@ extern "C" int nbcs_spline_pack_uv(const double* cu, const double* cv, int64_t n
 {
     if (n < 0 || (n > 0 && (!cu || !cv || !coef_uv)))
         return set_error(NBCS_ERR_INVALID, "pack_uv: bad arguments");
-    if ((reinterpret_cast<uintptr_t>(coef_uv) | reinterpret_cast<uintptr_t>(coef_uv32)) & 15)
-        return set_error(NBCS_ERR_INVALID, "pack_uv: outputs must be 16-byte aligned");
+    if ((reinterpret_cast<uintptr_t>(coef_uv) & 15) || (reinterpret_cast<uintptr_t>(coef_uv32) & 31))
+        return set_error(NBCS_ERR_INVALID,
+                         "pack_uv: coef_uv must be 16-byte and coef_uv32 32-byte aligned");
     if (n == 0) return NBCS_OK;
     long blocks = (n + 255) / 256;
     long cap = (long)sm_count() * 16;

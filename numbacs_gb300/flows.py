@@ -171,7 +171,7 @@ def get_flow_2D(grid_vel, C_eval_u, C_eval_v, spherical=0, extrap_mode="constant
         raise ValueError("coefficient arrays must have shape (nt+2, nx+2, ny+2)")
     n = cu.numel()
     uv = D.empty((n, 2))
-    uv32 = D.empty((n, 4), torch.float32)  # pair layout (u_k, v_k, u_k+1, v_k+1)
+    uv32 = D.empty((n, 8), torch.float32)  # quad layout (u_j, v_j), j = k .. k+3
     L = _lib.load()
     _lib.check(L.nbcs_spline_pack_uv(D.ptr(cu), D.ptr(cv), n, D.ptr(uv), D.ptr(uv32),
                                      D.stream_ptr()))
