@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--rtol", type=float, default=None, help="fixed rtol (skips the accuracy ladder)")
+    ap.add_argument("--lanes", type=int, default=None,
+                    help="fixed lanes per particle (with --blocks-per-sm: skips the autotuner)")
+    ap.add_argument("--blocks-per-sm", type=int, default=None)
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no ladder, plain comparison, e2e or CPU baseline)")
     return ap.parse_args()
@@ -287,8 +290,11 @@ def run_ours(args, rank, world):
 
     # launch shape (lanes per particle, grid cap) from the autotuner cache
     from numbacs_gb300.autotune import tune_flowmap
-    lanes, bps = tune_flowmap(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
-                              blocks=(0, 4, 6, 8))
+    if args.lanes is not None and args.blocks_per_sm is not None:
+        lanes, bps = args.lanes, args.blocks_per_sm
+    else:
+        lanes, bps = tune_flowmap(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision=prec,
+                                  blocks=(0, 4, 6, 8))
 
     def step(ev=None):
         if ev is not None:
@@ -416,7 +422,8 @@ def run_ours(args, rank, world):
 def run_batch(wl, rtol, steps):
     """Batched time series: 48 geophysical fields (t0 = 168 + k h, T ~ U[-120, -24] h,
     spacing in {0.1, 0.2, 0.4} deg) plus the Bickley jet on 1001 x 301 for 40 days, all
-    in one persistent launch replayed from a CUDA graph; against the same fields
+    in one launch replayed from a CUDA graph (schedule autotuned: persistent
+    work-stealing grid or one block per particle tile); against the same fields
     launched one flowmap_grid_2D + ftle_evec_2D call at a time."""
     import torch
     import numbacs_gb300 as nb
@@ -460,7 +467,9 @@ def run_batch(wl, rtol, steps):
             "blocks_per_sm": batch.blocks_per_sm, "ms_per_batch": ms_batch,
             "particles_per_s": n / (ms_batch * 1e-3), "fields_per_s": len(fields) / (ms_batch * 1e-3),
             "sequential_ms": ms_seq, "speedup_vs_sequential": ms_seq / ms_batch,
-            "launch": "one persistent integrator launch + one FTLE launch, CUDA graph replay"}
+            "schedule": ("one block per particle tile" if batch.blocks_per_sm < 0 else
+                         "persistent, %d blocks/SM, warps take chunks" % batch.blocks_per_sm),
+            "launch": "one integrator launch + one FTLE launch, CUDA graph replay"}
 
 
 def train_proposer(rtol, atol, seeds=range(8), t0s=(168.0, 190.0, 215.0), sample=0.15):

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define NBCS_ABI_VERSION 1
+#define NBCS_ABI_VERSION 2
 
 /* return codes */
 #define NBCS_OK 0
@@ -148,6 +148,7 @@ typedef struct nbcs_batch {
     int32_t nflows, nfields, precision, reserved;
     int64_t total_chunks; /* 32-particle work units over all fields */
     int64_t ftle_blocks;  /* 256-point FTLE work units */
+    int64_t tiles;        /* particle tiles of one 128-thread block over all fields */
 } nbcs_batch;
 
 size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields);
@@ -156,12 +157,16 @@ size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields);
 int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const nbcs_field* fields,
                        int32_t nfields, int32_t precision, void* scratch, size_t scratch_bytes,
                        nbcs_batch* plan, void* stream);
-/* Integrate every particle of every field in one persistent launch (warps
- * take 32-particle chunks from a shared counter, so fields of different sizes
- * and lengths balance across the GPU), then run the FTLE/eigvec stencil of all
- * fields in one launch.  Kernel launches only: capturable in a CUDA graph.
- * opts: precision is taken from the plan; blocks_per_sm sets the persistent
- * grid (0 = full occupancy); stats/step_model unused. */
+/* Integrate every particle of every field in one launch, then run the
+ * FTLE/eigvec stencil of all fields in one launch.  Kernel launches only:
+ * capturable in a CUDA graph.  Two schedules, chosen by opts->blocks_per_sm:
+ *   >= 0  persistent grid of blocks_per_sm blocks per SM (0 = full occupancy)
+ *         whose warps take 32-particle chunks from a shared counter;
+ *   <  0  (mixed precision) one block per particle tile of any field, the
+ *         hardware block scheduler balancing the tiles of all fields.
+ * Either way fields of different sizes and lengths share the GPU instead of
+ * each leaving it idle at the end of its own launch.  opts: precision is
+ * taken from the plan; stats/step_model unused. */
 int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, void* stream);
 
 /* ------------------------------------------------------------ diagnostics */

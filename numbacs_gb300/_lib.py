@@ -50,7 +50,7 @@ class NbcsBatch(ctypes.Structure):
     _fields_ = [("scratch", ctypes.c_void_p), ("nflows", ctypes.c_int32),
                 ("nfields", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("total_chunks", ctypes.c_int64),
-                ("ftle_blocks", ctypes.c_int64)]
+                ("ftle_blocks", ctypes.c_int64), ("tiles", ctypes.c_int64)]
 
 
 # name -> (restype, argtypes)

@@ -60,8 +60,11 @@ def _time(fn, reps=2):
     return best
 
 
-def tune_batch(batch, candidates=(2, 3, 4, 5, 6, 8), force=False):
-    """Blocks per SM for a prepared FTLEBatch (cached)."""
+def tune_batch(batch, candidates=None, force=False):
+    """Schedule for a prepared FTLEBatch (cached): blocks per SM of the
+    persistent grid, or -1 for one block per particle tile (mixed only)."""
+    if candidates is None:
+        candidates = (2, 3, 4, 5, 6, 8) + ((-1,) if batch.precision == "mixed" else ())
     kinds = sorted({(f.flow.kind, f.flow.spherical) for f in batch.fields})
     bucket = int(math.log2(max(1, batch.particles)))
     key = "batch/%s/%s/%s/%d" % (_gpu(), batch.precision, kinds, bucket)

@@ -55,9 +55,11 @@ class Field:
 class FTLEBatch:
     """A prepared batch of fields; ``run()`` recomputes every field in place.
 
-    ``precision`` is "mixed" or "fp64"; ``blocks_per_sm`` sets the persistent
-    grid (None: taken from the autotuner cache, tuning on first use; 0: full
-    occupancy); ``graph=True`` captures the run in a CUDA graph on first call.
+    ``precision`` is "mixed" or "fp64"; ``blocks_per_sm`` picks the schedule:
+    >= 0 a persistent grid of that many blocks per SM (0: full occupancy) whose
+    warps take particle chunks from a shared counter, -1 (mixed) one block per
+    particle tile of any field; None takes it from the autotuner cache, tuning
+    on first use.  ``graph=True`` captures the run in a CUDA graph on first call.
     """
 
     def __init__(self, fields, precision="mixed", blocks_per_sm=None, graph=True, max_steps=100000):

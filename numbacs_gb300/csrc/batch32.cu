@@ -19,6 +19,57 @@ namespace nbcs {
 
 __global__ void batch_reset_kernel(BatchHeader* hdr) { hdr->counter = 0ull; }
 
+// Integrate particle (i, j) of field F and write its flow map and status
+// (the group's leader lane writes).  `lane` is the thread's lane in its warp.
+__device__ __forceinline__ void batch_solve32(const DevFlow32* __restrict__ flows,
+                                              const DevField& F, int i, int j, int lane,
+                                              float2* kc, int nmax)
+{
+    const long p = (long)i * F.ny + j;
+    double r0 = 0.0, r1 = 0.0;
+    int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
+    if (!(F.mask && F.mask[p])) {
+        ParamsF P;
+#pragma unroll
+        for (int q = 0; q < NBCS_MAX_PARAMS; ++q) P.v[q] = (float)F.P.v[q];
+        const F2 xs = f2_from_double(F.ts), xe = f2_from_double(F.te);
+        const float rtol = (float)F.rtol, atol = (float)F.atol;
+        F2 yv[2] = {f2_from_double(F.x[i]), f2_from_double(F.y[j])};
+        const DevFlow32& fl = flows[F.flow];
+        switch (fl.kind) {
+        case NBCS_FLOW_DOUBLE_GYRE:
+            st = dop853_solve32(FlowDG32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
+            break;
+        case NBCS_FLOW_BICKLEY:
+            st = dop853_solve32(FlowBickley32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj,
+                                &nf);
+            break;
+        default:  // spline fields run two lanes per particle
+#define NBCS_SPLINE_SOLVE(SPH, LP)                                                              \
+    st = dop853_solve32(FlowSpline32<SPH, LP>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv, rtol,  \
+                    atol, nmax, kc, &a, &rj, &nf)
+            if (F.lp == 2) {
+                if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 2);
+                else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 2);
+                else NBCS_SPLINE_SOLVE(0, 2);
+            } else {
+                if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 1);
+                else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 1);
+                else NBCS_SPLINE_SOLVE(0, 1);
+            }
+#undef NBCS_SPLINE_SOLVE
+            break;
+        }
+        r0 = f2_to_double(yv[0]);
+        r1 = f2_to_double(yv[1]);
+    }
+    if ((lane % F.lp) == 0) {
+        reinterpret_cast<double2*>(F.out)[p] = make_double2(r0, r1);
+        if (F.status) F.status[p] = st;
+    }
+}
+
+// persistent schedule: warps take 32-particle chunks from the shared counter
 __global__ void __launch_bounds__(kBatchThreads)
 batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
                const DevField* __restrict__ fields, int nfields, int nmax)
@@ -32,53 +83,30 @@ batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
         if (lane == 0) c = atomicAdd(&hdr->counter, 1ull);
         c = __shfl_sync(0xffffffffu, c, 0);
         if ((long long)c >= total) break;
-        const int f = batch_find<true>(fields, nfields, (long long)c);
+        const int f = batch_find<kByChunk>(fields, nfields, (long long)c);
         const DevField& F = fields[f];
         int i, j;
         if (!batch_particle(F, (long long)c, lane, &i, &j)) continue;  // whole lane group
-        const long p = (long)i * F.ny + j;
-        double r0 = 0.0, r1 = 0.0;
-        int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
-        if (!(F.mask && F.mask[p])) {
-            ParamsF P;
-#pragma unroll
-            for (int q = 0; q < NBCS_MAX_PARAMS; ++q) P.v[q] = (float)F.P.v[q];
-            const F2 xs = f2_from_double(F.ts), xe = f2_from_double(F.te);
-            const float rtol = (float)F.rtol, atol = (float)F.atol;
-            F2 yv[2] = {f2_from_double(F.x[i]), f2_from_double(F.y[j])};
-            const DevFlow32& fl = flows[F.flow];
-            switch (fl.kind) {
-            case NBCS_FLOW_DOUBLE_GYRE:
-                st = dop853_solve32(FlowDG32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
-                break;
-            case NBCS_FLOW_BICKLEY:
-                st = dop853_solve32(FlowBickley32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj,
-                                    &nf);
-                break;
-            default:  // spline fields run two lanes per particle
-#define NBCS_SPLINE_SOLVE(SPH, LP)                                                              \
-    st = dop853_solve32(FlowSpline32<SPH, LP>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv, rtol,  \
-                        atol, nmax, kc, &a, &rj, &nf)
-                if (F.lp == 2) {
-                    if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 2);
-                    else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 2);
-                    else NBCS_SPLINE_SOLVE(0, 2);
-                } else {
-                    if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 1);
-                    else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 1);
-                    else NBCS_SPLINE_SOLVE(0, 1);
-                }
-#undef NBCS_SPLINE_SOLVE
-                break;
-            }
-            r0 = f2_to_double(yv[0]);
-            r1 = f2_to_double(yv[1]);
-        }
-        if ((lane % F.lp) == 0) {
-            reinterpret_cast<double2*>(F.out)[p] = make_double2(r0, r1);
-            if (F.status) F.status[p] = st;
-        }
+        batch_solve32(flows, F, i, j, lane, kc, nmax);
     }
+}
+
+// tile schedule: block b integrates block tile b of the concatenated fields
+// (the single-field kernel's (TI x 8) tiles and warp sub-tiles); the hardware
+// block scheduler starts a new tile wherever one finishes
+__global__ void __launch_bounds__(kBatchThreads)
+batch32_tiles_kernel(const DevFlow32* __restrict__ flows, const DevField* __restrict__ fields,
+                     int nfields, int nmax)
+{
+    __shared__ float2 ks[12 * kThreads32];
+    float2* kc = ks + threadIdx.x;
+    const long long b = blockIdx.x;
+    const DevField& F = fields[batch_find<kByTile>(fields, nfields, b)];
+    const long t = (long)(b - F.tile0) * kThreads32 + threadIdx.x;
+    int i, j;
+    const bool ok = F.lp == 2 ? tile_particle<2>(t, F.nx, F.ny, &i, &j)
+                              : tile_particle<1>(t, F.nx, F.ny, &i, &j);
+    if (ok) batch_solve32(flows, F, i, j, threadIdx.x & 31, kc, nmax);
 }
 
 static int persistent_blocks(const void* kernel, int threads, int blocks_per_sm)
@@ -100,6 +128,15 @@ int launch_batch32(const BatchHeader* dev_hdr, const DevFlow32* flows, const Dev
     NBCS_LAUNCH_CHECK();
     int blocks = persistent_blocks((const void*)batch32_kernel, kBatchThreads, blocks_per_sm);
     batch32_kernel<<<blocks, kBatchThreads, 0, s>>>(hdr, flows, fields, nfields, nmax);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+int launch_batch32_tiles(const DevFlow32* flows, const DevField* fields, int nfields,
+                         long long tiles, int nmax, cudaStream_t s)
+{
+    if (tiles > 0x7fffffffLL) return set_error(NBCS_ERR_UNSUPPORTED, "batch: too many tiles");
+    batch32_tiles_kernel<<<(unsigned)tiles, kBatchThreads, 0, s>>>(flows, fields, nfields, nmax);
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
@@ -149,7 +186,7 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         f32[k].deg_per_km = (float)(180.0 / (3.141592653589793 * fl.r));
         f64[k].r = fl.r;
     }
-    long long chunks = 0, blocks = 0;
+    long long chunks = 0, blocks = 0, tiles = 0;
     for (int k = 0; k < nfields; ++k) {
         const nbcs_field& F = fields[k];
         if (F.flow < 0 || F.flow >= nflows)
@@ -187,10 +224,13 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         D.lp = (precision == NBCS_PREC_MIXED && flows[F.flow].kind == NBCS_FLOW_SPLINE2D) ? 2 : 1;
         D.chunk0 = chunks;
         D.block0 = blocks;
+        D.tile0 = tiles;
         long n = (long)F.nx * F.ny;
         const int tj = batch_tile_j(D.lp);
         chunks += (long long)((F.nx + kBatchTileI - 1) / kBatchTileI) * ((F.ny + tj - 1) / tj);
         if (F.ftle) blocks += (n + kFtleBlock - 1) / kFtleBlock;
+        const int ti = kThreads32 / D.lp / 8;  // block tile: (ti x 8) particles
+        tiles += (long long)((F.nx + ti - 1) / ti) * ((F.ny + 7) / 8);
     }
     hdr->counter = 0;
     hdr->total_chunks = chunks;
@@ -206,6 +246,7 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
     plan->reserved = 0;
     plan->total_chunks = chunks;
     plan->ftle_blocks = blocks;
+    plan->tiles = tiles;
     return NBCS_OK;
 }
 
@@ -221,9 +262,11 @@ extern "C" int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, voi
     cudaStream_t s = as_stream(stream);
     int rc;
     if (plan->total_chunks > 0) {
-        if (plan->precision == NBCS_PREC_MIXED)
-            rc = launch_batch32(hdr, reinterpret_cast<const DevFlow32*>(base + lay.off_f32), fields,
-                                plan->nfields, bps, nmax, s);
+        const DevFlow32* f32 = reinterpret_cast<const DevFlow32*>(base + lay.off_f32);
+        if (plan->precision == NBCS_PREC_MIXED && bps < 0)
+            rc = launch_batch32_tiles(f32, fields, plan->nfields, plan->tiles, nmax, s);
+        else if (plan->precision == NBCS_PREC_MIXED)
+            rc = launch_batch32(hdr, f32, fields, plan->nfields, bps, nmax, s);
         else
             rc = launch_batch64(hdr, reinterpret_cast<const DevFlow64*>(base + lay.off_f64), fields,
                                 plan->nfields, bps, nmax, s);

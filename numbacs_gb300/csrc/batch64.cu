@@ -22,7 +22,7 @@ batch64_kernel(BatchHeader* hdr, const DevFlow64* __restrict__ flows,
         if (lane == 0) c = atomicAdd(&hdr->counter, 1ull);
         c = __shfl_sync(0xffffffffu, c, 0);
         if ((long long)c >= total) break;
-        const int f = batch_find<true>(fields, nfields, (long long)c);
+        const int f = batch_find<kByChunk>(fields, nfields, (long long)c);
         const DevField& F = fields[f];
         int i, j;
         if (!batch_particle(F, (long long)c, lane, &i, &j)) continue;

@@ -54,7 +54,7 @@ struct DevField {
     int32_t* status;
     double* ftle;
     double* evec;
-    long long chunk0, block0;
+    long long chunk0, block0, tile0;  // prefixes of chunks, FTLE blocks, block tiles
 };
 
 inline size_t batch_align(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -73,14 +73,17 @@ inline BatchLayout batch_layout(int nflows, int nfields)
     return L;
 }
 
-// index of the last field whose prefix value is <= c
-template <bool CHUNKS>
+enum BatchKey { kByChunk, kByFtleBlock, kByTile };
+
+// index of the last field whose prefix value (chunk0, block0 or tile0) is <= c
+template <BatchKey KEY>
 __device__ __forceinline__ int batch_find(const DevField* __restrict__ fields, int nf, long long c)
 {
     int lo = 0, hi = nf - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        long long v = CHUNKS ? fields[mid].chunk0 : fields[mid].block0;
+        long long v = KEY == kByChunk ? fields[mid].chunk0
+                    : KEY == kByFtleBlock ? fields[mid].block0 : fields[mid].tile0;
         if (v <= c) lo = mid;
         else hi = mid - 1;
     }
@@ -102,6 +105,8 @@ __device__ __forceinline__ bool batch_particle(const DevField& F, long long c, i
     return *i < F.nx && *j < F.ny;
 }
 
+int launch_batch32_tiles(const DevFlow32* flows, const DevField* fields, int nfields,
+                         long long tiles, int nmax, cudaStream_t s);
 int launch_batch32(const BatchHeader* dev_hdr, const DevFlow32* flows, const DevField* fields,
                    int nfields, int blocks_per_sm, int nmax, cudaStream_t s);
 int launch_batch64(const BatchHeader* dev_hdr, const DevFlow64* flows, const DevField* fields,

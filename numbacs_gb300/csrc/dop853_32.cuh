@@ -241,18 +241,25 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
 
 // Thread -> (particle group, lane) map.  A block of kThreads32 threads holds
 // kThreads32/LP particles laid out as a (TI x 8) tile of the grid; tiles run
-// in row-major order.
+// in row-major order.  Inside the tile each warp takes a compact (WI x WJ)
+// sub-tile (4 x 8, 4 x 4, 2 x 4 particles at LP = 1, 2, 4): the fewer spline
+// cells a warp's particles sit in, the more of its stencil gathers hit the
+// same 32-byte entries.
 template <int LP>
 __device__ __forceinline__ bool tile_particle(long t, int nx, int ny, int* i, int* j)
 {
     constexpr int PB = kThreads32 / LP, TJ = 8, TI = PB / TJ;
+    constexpr int PW = 32 / LP;                     // particles per warp
+    constexpr int WJ = LP == 1 ? 8 : 4, WI = PW / WJ;
+    constexpr int WPJ = TJ / WJ;                    // warps along j
     long tile = t / kThreads32;
     int r = (int)(t - tile * kThreads32) / LP;
+    int w = r / PW, q = r - w * PW;
     int tiles_j = (ny + TJ - 1) / TJ;
     long ti = tile / tiles_j;
     int tj = (int)(tile - ti * tiles_j);
-    *i = (int)(ti * TI) + r / TJ;
-    *j = tj * TJ + (r % TJ);
+    *i = (int)(ti * TI) + (w / WPJ) * WI + q / WJ;
+    *j = tj * TJ + (w % WPJ) * WJ + q % WJ;
     return *i < nx && *j < ny;
 }
 

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kFtleBlock)
 ftle_batch_kernel(const DevField* __restrict__ fields, int nfields, long long total_blocks)
 {
     for (long long b = blockIdx.x; b < total_blocks; b += gridDim.x) {
-        const int f = batch_find<false>(fields, nfields, b);
+        const int f = batch_find<kByFtleBlock>(fields, nfields, b);
         const DevField& F = fields[f];
         const long n = (long)F.nx * F.ny;
         const long k = (long)(b - F.block0) * kFtleBlock + threadIdx.x;

@@ -123,7 +123,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
         if (PROPOSE) {
             const bool want = active && fresh;
             if (__any_sync(FULL, want)) {
-                const float lh = mlp_predict_warp(*W, feat, xs, outs);
+                const float lh = mlp_predict_groups<Flow::LP>(*W, feat, xs, outs);
                 if (want) {
                     const float hm = __expf(lh), hc = fabsf(h);
                     float hn = mode == 0 ? hm : (mode == 1 ? fminf(hm, hc) : sqrtf(hm * hc));
@@ -242,6 +242,9 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
     *status_out = status;
 }
 
+// No register cap: capping at 72 (7 blocks/SM) spills onto the L1 pipe that
+// the spline gathers already saturate and measured 36% slower than the
+// uncapped 96 registers.
 template <class Flow, bool LOG, bool PROPOSE>
 __global__ void __launch_bounds__(kThreads32)
 learned_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restrict__ x,

@@ -167,27 +167,108 @@ __device__ __forceinline__ void mlp_put_features(const MlpBlob& W, const float* 
     for (int i = kMlpIn; i < kMlpInPad; ++i) row[i] = __float2bfloat16_rn(0.f);
 }
 
+// Inference-only forward pass of rows 0 .. 16*MT-1 of xs into outs[row] (net
+// output before the target de-standardisation).  Same arithmetic, in the same
+// order, as mlp_hidden + mlp_out_rows, but layer 2 runs one n-tile at a time
+// straight into the output dot product, so only the layer-1 A fragments stay
+// live (~40 registers instead of ~100: this sits inside the integrator loop,
+// where registers decide occupancy).
+template <int MT>
+__device__ __forceinline__ void mlp_rows(const MlpBlob& W, const __nv_bfloat16* xs, float* outs)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt) {
+        uint32_t ax[4];
+        const __nv_bfloat16* r0 = xs + (mt * 16 + g) * kMlpInPad + 2 * t;
+        const __nv_bfloat16* r1 = r0 + 8 * kMlpInPad;
+        ax[0] = *reinterpret_cast<const uint32_t*>(r0);
+        ax[1] = *reinterpret_cast<const uint32_t*>(r1);
+        ax[2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+        ax[3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+        uint32_t a1[4][4];
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            float c[2][4];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int nt = 2 * ks + h;
+                const float bb0 = W.k.b1[nt * 8 + 2 * t], bb1 = W.k.b1[nt * 8 + 2 * t + 1];
+                c[h][0] = bb0;
+                c[h][1] = bb1;
+                c[h][2] = bb0;
+                c[h][3] = bb1;
+                uint32_t b[2];
+                load_b_frag(W.w1, kMlpInPad, nt, 0, b);
+                mma_bf16_16816(c[h], ax, b);
+            }
+            a1[ks][0] = pack_bf16(fmaxf(c[0][0], 0.f), fmaxf(c[0][1], 0.f));
+            a1[ks][1] = pack_bf16(fmaxf(c[0][2], 0.f), fmaxf(c[0][3], 0.f));
+            a1[ks][2] = pack_bf16(fmaxf(c[1][0], 0.f), fmaxf(c[1][1], 0.f));
+            a1[ks][3] = pack_bf16(fmaxf(c[1][2], 0.f), fmaxf(c[1][3], 0.f));
+        }
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const float bb0 = W.k.b2[nt * 8 + 2 * t], bb1 = W.k.b2[nt * 8 + 2 * t + 1];
+            float c[4] = {bb0, bb1, bb0, bb1};
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                uint32_t b[2];
+                load_b_frag(W.w2, kMlpHid, nt, ks, b);
+                mma_bf16_16816(c, a1[ks], b);
+            }
+            const float w0 = W.k.w3[nt * 8 + 2 * t], w1 = W.k.w3[nt * 8 + 2 * t + 1];
+            s0 = fmaf(fmaxf(c[0], 0.f), w0, fmaf(fmaxf(c[1], 0.f), w1, s0));
+            s1 = fmaf(fmaxf(c[2], 0.f), w0, fmaf(fmaxf(c[3], 0.f), w1, s1));
+        }
+        s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+        s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+        if (t == 0) {
+            outs[mt * 16 + g] = s0 + W.k.b3;
+            outs[mt * 16 + g + 8] = s1 + W.k.b3;
+        }
+    }
+}
+
 // Whole-warp inference: every lane passes its features, gets its prediction
 // (in target units: out_mu + out_sigma * net).  All 32 lanes must call it.
 __device__ __forceinline__ float mlp_predict_warp(const MlpBlob& W, const float* feat,
                                                   __nv_bfloat16* xs, float* outs)
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int lane = threadIdx.x & 31;
     mlp_put_features(W, feat, xs);
     __syncwarp();
-    float h2[2][8][4];
-    uint32_t a1[2][4][4];
-    mlp_hidden(W, xs, h2, a1);
-    float o[2][2];
-    mlp_out_rows(W, h2, o);
-    if (t == 0) {
-        outs[g] = o[0][0];
-        outs[g + 8] = o[0][1];
-        outs[16 + g] = o[1][0];
-        outs[24 + g] = o[1][1];
-    }
+    mlp_rows<2>(W, xs, outs);
     __syncwarp();
     float r = fmaf(W.k.out_sigma, outs[lane], W.k.out_mu);
+    __syncwarp();
+    return r;
+}
+
+// Inference for a warp whose lane groups of LP lanes share one sample: the
+// group leader's features go to row lane / LP, so 32 / LP rows (one 16-row
+// tile for LP >= 2) are evaluated.  All 32 lanes must call it; every lane of
+// a group gets the group's prediction.
+template <int LP>
+__device__ __forceinline__ float mlp_predict_groups(const MlpBlob& W, const float* feat,
+                                                    __nv_bfloat16* xs, float* outs)
+{
+    const int lane = threadIdx.x & 31;
+    if ((lane & (LP - 1)) == 0) {
+        __nv_bfloat16* row = xs + (lane / LP) * kMlpInPad;
+#pragma unroll
+        for (int i = 0; i < kMlpIn; ++i)
+            row[i] = __float2bfloat16_rn((feat[i] - W.k.mu[i]) * W.k.inv_sigma[i]);
+#pragma unroll
+        for (int i = kMlpIn; i < kMlpInPad; ++i) row[i] = __float2bfloat16_rn(0.f);
+    }
+    __syncwarp();
+    mlp_rows<(32 / LP + 15) / 16>(W, xs, outs);
+    __syncwarp();
+    float r = fmaf(W.k.out_sigma, outs[lane / LP], W.k.out_mu);
     __syncwarp();
     return r;
 }

@@ -37,10 +37,11 @@ def _fields(nb):
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("graph", [False, True])
-def test_batch_equals_single_field(nb, precision, graph):
+@pytest.mark.parametrize("schedule", [3, -1])
+def test_batch_equals_single_field(nb, precision, graph, schedule):
     from numbacs_gb300.batch import FTLEBatch
     fields = _fields(nb)
-    b = FTLEBatch(fields, precision=precision, blocks_per_sm=3, graph=graph)
+    b = FTLEBatch(fields, precision=precision, blocks_per_sm=schedule, graph=graph)
     b.run()
     b.run()  # a second run (graph replay) recomputes the same values
     torch.cuda.synchronize()
@@ -61,7 +62,7 @@ def test_batch_autotune_and_sizes(nb):
     from numbacs_gb300.batch import FTLEBatch
     fields = _fields(nb)
     b = FTLEBatch(fields, precision="mixed", blocks_per_sm=None, graph=True)
-    assert b.blocks_per_sm >= 1
+    assert b.blocks_per_sm >= 1 or b.blocks_per_sm == -1
     b.run()
     torch.cuda.synchronize()
     assert b.particles == sum(f.x.numel() * f.y.numel() for f in fields)
@@ -69,3 +70,7 @@ def test_batch_autotune_and_sizes(nb):
         tj = 4 if f.flow.kind == 2 else 8
         return -(-f.x.numel() // 4) * -(-f.y.numel() // tj)
     assert int(b.plan.total_chunks) == sum(units(f) for f in fields)
+    def tiles(f):  # one 128-thread block: (16 x 8) particles, (8 x 8) at two lanes each
+        ti = 8 if f.flow.kind == 2 else 16
+        return -(-f.x.numel() // ti) * -(-f.y.numel() // 8)
+    assert int(b.plan.tiles) == sum(tiles(f) for f in fields)
