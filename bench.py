@@ -381,6 +381,14 @@ def run_ours(args, rank, world):
     achieved = flops_launch / (fm_ms * 1e-3) / 1e12
     peak = peak32 if prec == "mixed" else peak64
     traffic = _profile_traffic(prec)
+    # the spline RHS gathers 4x4x4 (u, v) coefficients: 512 B in FP32, 1 KB in FP64
+    gather_b = float(((att * 12 + 2) * (512 if prec == "mixed" else 1024)).sum())
+    hbm_peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            hbm_peak = json.load(fh).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -399,7 +407,12 @@ def run_ours(args, rank, world):
                      "traffic": traffic,
                      "peak_source": "in-run FMA probe (nbcs_probe_fma), burst",
                      "kernel": "flowmap32_kernel" if prec == "mixed" else "flowmap64_kernel",
-                     "flops_per_launch": flops_launch, "launch_ms": fm_ms},
+                     "flops_per_launch": flops_launch, "launch_ms": fm_ms,
+                     "gather": {"bytes_per_launch": gather_b,
+                                "achieved_gbs": gather_b / (fm_ms * 1e-3) / 1e9,
+                                "hbm_peak_gbs_measured": hbm_peak,
+                                "note": "coefficient gathers are served by L1/L2; DRAM bytes "
+                                        "per launch are roofline.traffic"}},
         "learned": learned,
         "breakdown_ms": {"flowmap": fm_ms, "ftle_evec": sum(t_ftle) / len(t_ftle),
                          "ridge": sum(t_ridge) / len(t_ridge)},
