@@ -120,6 +120,35 @@ int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T,
                          const uint8_t* mask, double* flowmap, int32_t* status,
                          const nbcs_opts* opts, void* stream);
 
+/* flowmap_aux_grid_2D (integration.py:249-464) with method="dop853": every
+ * grid point (x[i], y[j]) integrates the particles started at (x[i], y[j]) +
+ * (h,0), (-h,0), (0,h), (0,-h) and, with eig_main, (0,0), into flowmap_aux
+ * (nx, ny, 5 or 4, 2).  compute_edge != 0: edge points integrate only their
+ * centre particle (eig_main) or all four; compute_edge == 0: edge points are
+ * skipped.  Masked and skipped entries are left 0 with status MASKED;
+ * status (nx, ny, 5 or 4) int32 may be NULL.  opts as for
+ * nbcs_flowmap_grid_2d (no step_model; the mixed path's FP32 stage rounding
+ * is amplified 1/(2h)-fold by C_eig_aux_2D's differences, so FP64 is the
+ * path for this one). */
+int nbcs_flowmap_aux_grid_2d(const nbcs_flow* flow, double t0, double T,
+                             const double* x, int32_t nx, const double* y, int32_t ny,
+                             const double* params, int32_t np, double h, int32_t eig_main,
+                             int32_t compute_edge, double rtol, double atol,
+                             const uint8_t* mask, double* flowmap_aux, int32_t* status,
+                             const nbcs_opts* opts, void* stream);
+
+/* flowmap_composition (integration.py:609-641): compose nT flow maps
+ * (nT, nx, ny, 2) on the grid `grid` (host, 6 doubles: x0, x1, nx, y0, y1, ny
+ * -- the UCGrid tuple) into out (nx, ny, 2).  Map j of the sequence is
+ * flowmaps[(first + j) % nT] (pass first = 0 for the reference's order; a
+ * ring buffer advanced by one map per step needs no shifting).  Bilinear
+ * interpolation, 0 outside the grid box (interpolation's xto.CONSTANT); nT = 1
+ * interpolates the map at its own values, as the reference does.  The
+ * callers flowmap_composition_initial / _step (:644-737) are host loops over
+ * nbcs_flowmap_grid_2d and this call. */
+int nbcs_flowmap_compose(const double* flowmaps, int32_t nT, int32_t first, const double* grid,
+                         double* out, void* stream);
+
 /* -------------------------------------------------------- batched fields */
 
 /* One FTLE field of a batched launch: what one flowmap_grid_2D call (plus an
@@ -179,6 +208,16 @@ int nbcs_ftle_grid_2d(const double* flowmap, int32_t nx, int32_t ny, double T, d
  * (nx,ny,2,2) eigenvectors in columns. */
 int nbcs_c_eig_2d(const double* flowmap, int32_t nx, int32_t ny, double dx, double dy,
                   const uint8_t* mask, double* evals, double* evecs, void* stream);
+
+/* C_eig_aux_2D (diagnostics.py:113-197): flowmap_aux (nx, ny, 5 or 4, 2) from
+ * nbcs_flowmap_aux_grid_2d -> evals (nx,ny,2) ascending, evecs (nx,ny,2,2)
+ * eigenvectors in columns.  eig_main: eigenvectors from the aux-particle
+ * differences (spacing h), eigenvalues from the centre particles' main-grid
+ * differences (dx, dy), at 2 <= i < nx-2, 2 <= j < ny-2; otherwise both from
+ * the aux differences at 1 <= i < nx-1, 1 <= j < ny-1; 0 elsewhere. */
+int nbcs_c_eig_aux_2d(const double* flowmap_aux, int32_t nx, int32_t ny, int32_t eig_main,
+                      double dx, double dy, double h, const uint8_t* mask, double* evals,
+                      double* evecs, void* stream);
 
 /* ftle_from_eig (diagnostics.py:247-269) on a strided eigenvalue array:
  * ftle[k] = log(ev[k*stride]) / (2|T|) if ev > 1 else 0. */

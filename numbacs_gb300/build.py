@@ -39,6 +39,7 @@ SOURCES = [
     ("mlp_train.cu", []),
     ("learned.cu", []),
     ("label.cu", []),
+    ("compose.cu", ["-fmad=false"]),
 ]
 
 

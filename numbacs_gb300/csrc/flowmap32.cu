@@ -25,9 +25,10 @@ namespace nbcs {
 template <class Flow>
 __global__ void __launch_bounds__(kThreads32)
 flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restrict__ x,
-                 const double* __restrict__ y, int nx, int ny, const uint8_t* __restrict__ mask,
-                 double* __restrict__ out, int32_t* __restrict__ status,
-                 int32_t* __restrict__ stats, float rtol, float atol, int nmax, long nthreads)
+                 const double* __restrict__ y, int nx, int nyv, AuxGrid aux,
+                 const uint8_t* __restrict__ mask, double* __restrict__ out,
+                 int32_t* __restrict__ status, int32_t* __restrict__ stats, float rtol,
+                 float atol, int nmax, long nthreads)
 {
     constexpr int LP = Flow::LP;
     __shared__ float2 ks[12 * kThreads32];
@@ -37,12 +38,12 @@ flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restr
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nthreads;
          t += (long)gridDim.x * blockDim.x) {
         int i, j;
-        if (!tile_particle<LP>(t, nx, ny, &i, &j)) continue;
-        long k = (long)i * ny + j;
-        double r0 = 0.0, r1 = 0.0;
+        if (!tile_particle<LP>(t, nx, nyv, &i, &j)) continue;
+        long k = (long)i * nyv + j;
+        double r0 = 0.0, r1 = 0.0, x0, y0;
         int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
-        if (!(mask && mask[k])) {
-            F2 yv[2] = {f2_from_double(x[i]), f2_from_double(y[j])};
+        if (particle_start(aux, x, y, mask, nx, i, j, &x0, &y0)) {
+            F2 yv[2] = {f2_from_double(x0), f2_from_double(y0)};
             st = dop853_solve32(fl, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
             r0 = f2_to_double(yv[0]);
             r1 = f2_to_double(yv[1]);
@@ -134,7 +135,7 @@ struct Launch32 {
         constexpr int LP = Flow::LP;
         constexpr int PB = kThreads32 / LP;  // particles per block
         constexpr int TI = PB / 8;
-        long tiles = (long)((a->nx + TI - 1) / TI) * ((a->ny + 7) / 8);
+        long tiles = (long)((a->nx + TI - 1) / TI) * ((a->nyv() + 7) / 8);
         long nthreads = tiles * kThreads32;
         long blocks = tiles;
         if (a->blocks_per_sm > 0) {
@@ -143,7 +144,7 @@ struct Launch32 {
         }
         if (blocks > (1L << 30)) blocks = 1L << 30;
         flowmap32_kernel<<<(unsigned)blocks, kThreads32, 0, a->stream>>>(
-            fl, to_float(a->P), a->ts, a->te, a->x, a->y, a->nx, a->ny, a->mask, a->out,
+            fl, to_float(a->P), a->ts, a->te, a->x, a->y, a->nx, a->nyv(), a->aux, a->mask, a->out,
             a->status, a->stats, (float)a->rtol, (float)a->atol, a->nmax, nthreads);
         NBCS_LAUNCH_CHECK();
         return NBCS_OK;
@@ -169,7 +170,7 @@ struct LaunchRhs32 {
 
 int launch_flowmap32(const nbcs_flow* flow, const FlowmapArgs& a)
 {
-    int lp = spline_lanes(a.lanes, (long)a.nx * a.ny);
+    int lp = spline_lanes(a.lanes, (long)a.nx * a.nyv());
     return dispatch32(flow, lp, Launch32{&a});
 }
 

@@ -12,22 +12,23 @@ namespace nbcs {
 template <class Flow>
 __global__ void __launch_bounds__(kThreads64)
 flowmap64_kernel(Flow fl, Params P, double ts, double te, const double* __restrict__ x,
-                 const double* __restrict__ y, int nx, int ny, const uint8_t* __restrict__ mask,
-                 double* __restrict__ out, int32_t* __restrict__ status,
-                 int32_t* __restrict__ stats, double rtol, double atol, int nmax)
+                 const double* __restrict__ y, int nx, int nyv, AuxGrid aux,
+                 const uint8_t* __restrict__ mask, double* __restrict__ out,
+                 int32_t* __restrict__ status, int32_t* __restrict__ stats, double rtol,
+                 double atol, int nmax)
 {
     __shared__ double2 ks[12 * kThreads64];
     double2* kc = ks + threadIdx.x;
-    const long n = (long)nx * ny;
+    const long n = (long)nx * nyv;
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += (long)gridDim.x * blockDim.x) {
-        int i = (int)(k / ny), j = (int)(k - (long)i * ny);
-        double yv[2] = {0.0, 0.0};
+        int i = (int)(k / nyv), j = (int)(k - (long)i * nyv);
+        double yv[2] = {0.0, 0.0}, x0, y0;
         int st = NBCS_PARTICLE_MASKED;
         Dop853Stats s = {0, 0, 0};
-        if (!(mask && mask[k])) {
-            yv[0] = x[i];
-            yv[1] = y[j];
+        if (particle_start(aux, x, y, mask, nx, i, j, &x0, &y0)) {
+            yv[0] = x0;
+            yv[1] = y0;
             st = dop853_solve64(fl, P, ts, te, yv, rtol, atol, nmax, kc, &s);
         }
         reinterpret_cast<double2*>(out)[k] = make_double2(yv[0], yv[1]);
@@ -58,7 +59,7 @@ struct Launch64 {
     template <class Flow>
     int operator()(const Flow& fl) const
     {
-        const long n = (long)a->nx * a->ny;
+        const long n = (long)a->nx * a->nyv();
         const int threads = kThreads64;  // the stage-derivative columns are sized for it
         long blocks = (n + threads - 1) / threads;
         if (a->blocks_per_sm > 0) {
@@ -67,8 +68,8 @@ struct Launch64 {
         }
         if (blocks > (1L << 30)) blocks = 1L << 30;
         flowmap64_kernel<<<(unsigned)blocks, threads, 0, a->stream>>>(
-            fl, a->P, a->ts, a->te, a->x, a->y, a->nx, a->ny, a->mask, a->out, a->status,
-            a->stats, a->rtol, a->atol, a->nmax);
+            fl, a->P, a->ts, a->te, a->x, a->y, a->nx, a->nyv(), a->aux, a->mask, a->out,
+            a->status, a->stats, a->rtol, a->atol, a->nmax);
         NBCS_LAUNCH_CHECK();
         return NBCS_OK;
     }
@@ -133,11 +134,45 @@ extern "C" int nbcs_eval_rhs(const nbcs_flow* flow, const double* params, int32_
     return dispatch64(flow, LaunchRhs64{P, ty, (long)n, dy, as_stream(stream)});
 }
 
+static int flowmap_particles(const nbcs_flow* flow, double t0, double T, const double* x,
+                             int32_t nx, const double* y, int32_t ny, const double* params,
+                             int32_t np, double rtol, double atol, const uint8_t* mask,
+                             double* flowmap, int32_t* status, const nbcs_opts* opts,
+                             void* stream, const AuxGrid& aux);
+
 extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, const double* x,
                                     int32_t nx, const double* y, int32_t ny,
                                     const double* params, int32_t np, double rtol, double atol,
                                     const uint8_t* mask, double* flowmap, int32_t* status,
                                     const nbcs_opts* opts, void* stream)
+{
+    const AuxGrid plain = {0, ny, 1, 0.0};
+    return flowmap_particles(flow, t0, T, x, nx, y, ny, params, np, rtol, atol, mask, flowmap,
+                             status, opts, stream, plain);
+}
+
+extern "C" int nbcs_flowmap_aux_grid_2d(const nbcs_flow* flow, double t0, double T,
+                                        const double* x, int32_t nx, const double* y, int32_t ny,
+                                        const double* params, int32_t np, double h,
+                                        int32_t eig_main, int32_t compute_edge, double rtol,
+                                        double atol, const uint8_t* mask, double* flowmap_aux,
+                                        int32_t* status, const nbcs_opts* opts, void* stream)
+{
+    if (!(h > 0.0) && !(h < 0.0)) return set_error(NBCS_ERR_INVALID, "aux grid: h must be nonzero");
+    if (opts && opts->step_model)
+        return set_error(NBCS_ERR_UNSUPPORTED, "aux grid: no step_model");
+    if ((long)nx * ny * (eig_main ? 5 : 4) > 0x7fffffffL)
+        return set_error(NBCS_ERR_INVALID, "aux grid: too many particles");
+    const AuxGrid aux = {eig_main ? 5 : 4, ny, compute_edge ? 1 : 0, h};
+    return flowmap_particles(flow, t0, T, x, nx, y, ny, params, np, rtol, atol, mask,
+                             flowmap_aux, status, opts, stream, aux);
+}
+
+static int flowmap_particles(const nbcs_flow* flow, double t0, double T, const double* x,
+                             int32_t nx, const double* y, int32_t ny, const double* params,
+                             int32_t np, double rtol, double atol, const uint8_t* mask,
+                             double* flowmap, int32_t* status, const nbcs_opts* opts,
+                             void* stream, const AuxGrid& aux)
 {
     nbcs_opts o = {};
     o.precision = NBCS_PREC_FP64;
@@ -163,6 +198,7 @@ extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, 
     a.y = y;
     a.nx = nx;
     a.ny = ny;
+    a.aux = aux;
     a.mask = mask;
     a.out = flowmap;
     a.status = status;

@@ -5,12 +5,50 @@
 
 namespace nbcs {
 
+// The particle set of one launch: the grid (x_i, y_j) of flowmap_grid_2D, or
+// the auxiliary grid of flowmap_aux_grid_2D (integration.py:249-464) -- n = 5
+// (eig_main) or 4 particles per grid point, started at (x_i, y_j) + (h, 0),
+// (-h, 0), (0, h), (0, -h) [, (0, 0)] -- laid out as a virtual (nx, ny * n)
+// grid, so that the (nx, ny, n, 2) result is that grid's flow map and the
+// near-identical trajectories of one point sit in neighbouring lanes.
+struct AuxGrid {
+    int n;             // 0: plain grid; else 4 or 5 particles per grid point
+    int ny;            // columns of the real grid
+    int compute_edge;  // integrate the edge points (only their centre particle when n = 5)
+    double h;
+};
+
+// Start point of particle (i, jv) of the virtual grid; false when it is masked
+// or skipped (its result stays 0 with status MASKED, as the reference leaves
+// those entries of its zero-initialised output).
+__device__ __forceinline__ bool particle_start(const AuxGrid& A, const double* __restrict__ x,
+                                               const double* __restrict__ y,
+                                               const uint8_t* __restrict__ mask, int nx, int i,
+                                               int jv, double* x0, double* y0)
+{
+    if (A.n == 0) {
+        if (mask && mask[(long)i * A.ny + jv]) return false;
+        *x0 = x[i];
+        *y0 = y[jv];
+        return true;
+    }
+    const int j = jv / A.n, k = jv - j * A.n;
+    if (mask && mask[(long)i * A.ny + j]) return false;
+    const bool edge = i == 0 || i == nx - 1 || j == 0 || j == A.ny - 1;
+    if (edge && !(A.compute_edge && (A.n == 4 || k == 4))) return false;
+    // np.array([x[i], y[j]]) + aux_grid[k, :]
+    *x0 = x[i] + (k == 0 ? A.h : k == 1 ? -A.h : 0.0);
+    *y0 = y[j] + (k == 2 ? A.h : k == 3 ? -A.h : 0.0);
+    return true;
+}
+
 struct FlowmapArgs {
     Params P;
     double ts, te;  // solver-time span params[0] * [t0, t0 + T]
     const double* x;
     const double* y;
-    int nx, ny;
+    int nx, ny;  // real grid
+    AuxGrid aux;
     const uint8_t* mask;
     double* out;
     int32_t* status;
@@ -20,6 +58,8 @@ struct FlowmapArgs {
     int threads, blocks_per_sm, lanes;
     const void* step_model;
     cudaStream_t stream;
+    // columns of the virtual particle grid
+    int nyv() const { return aux.n ? ny * aux.n : ny; }
 };
 
 int launch_flowmap64(const nbcs_flow* flow, const FlowmapArgs& a);

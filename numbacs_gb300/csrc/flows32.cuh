@@ -83,10 +83,11 @@ struct FlowBickley32 {
     }
 };
 
-// One spline axis: node k sits at a + k*d, with a and d kept as float pairs
-// (hi + lo) so node positions can be rebuilt to ~2^-48 relative accuracy.
+// One spline axis: node k sits at a + k*d, with a, d and the far end b kept as
+// float pairs (hi + lo) so node positions can be rebuilt to ~2^-48 relative
+// accuracy and the box test is exact in its sign.
 struct AxisF {
-    float a_h, a_l, d_h, d_l, dinv;
+    float a_h, a_l, d_h, d_l, dinv, b_h, b_l;
     int n;
 };
 
@@ -108,6 +109,8 @@ inline SplineGridF make_grid_f(const double* g)
         A.d_h = (float)dd;
         A.d_l = (float)(dd - (double)A.d_h);
         A.dinv = (float)((double)(n - 1) / (b - a));
+        A.b_h = (float)b;
+        A.b_l = (float)(b - (double)A.b_h);
         A.n = n;
     }
     s.sx = s.ax[2].n + 2;
@@ -118,9 +121,13 @@ inline SplineGridF make_grid_f(const double* g)
 // Cell index and offset t of the coordinate vh + vs on one axis.  The cell is
 // picked from the rounded coordinate, the offset is formed from the pair
 // (so t may sit a rounding error outside [0, 1] next to a knot, where the two
-// cubic pieces agree), and extrap_mode "constant" clamps the *precise* offset
-// at the two ends of the grid so the clamped field stays continuous.
-__device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, float* t)
+// cubic pieces agree).  A coordinate strictly outside [a, b] sets *outside
+// (extrap_mode "constant": the interpolant is 0 there).  That test subtracts
+// the ends as pairs -- the hi parts cancel exactly next to an end -- so its
+// sign is the FP64 path's: a particle grid that overshoots the box by 1e-12
+// (np.arange end points) starts outside on both paths.
+__device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, float* t,
+                                           bool* outside)
 {
     float u = ((vh + vs) - A.a_h) * A.dinv;
     if (u != u) { *t = u; return 0; }  // NaN propagates
@@ -136,10 +143,12 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
     float err = __fadd_rn(__fsub_rn(A.a_h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
     float lo = err + (e + A.a_l);
     float r = __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
-    float tt = r * A.dinv;
-    if (i == 0) tt = fmaxf(tt, 0.0f);
-    if (i == A.n - 2) tt = fminf(tt, 1.0f);
-    *t = tt;
+    *t = r * A.dinv;
+    if (i == 0) {
+        if (__fadd_rn(__fsub_rn(vh, A.a_h), __fsub_rn(vs, A.a_l)) < 0.0f) *outside = true;
+    } else if (i == A.n - 2) {
+        if (__fadd_rn(__fsub_rn(vh, A.b_h), __fsub_rn(vs, A.b_l)) > 0.0f) *outside = true;
+    }
     return i;
 }
 
@@ -311,9 +320,15 @@ struct FlowSpline32 {
             if (k != 0.0f) xh = fmaf(-360.0f, k, xh);
         }
         float ft, fx, fy, wx[4], wy[4];
-        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft);
-        int ix = locate_pair(g.ax[1], xh, ys[0], &fx);
-        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy);
+        bool out = false;
+        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft, &out);
+        int ix = locate_pair(g.ax[1], xh, ys[0], &fx, &out);
+        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy, &out);
+        if (out) {  // the lanes of a group agree: they hold the same particle
+            dy[0] = 0.0f;
+            dy[1] = 0.0f;
+            return;
+        }
         bspline_w32(fx, wx);
         bspline_w32(fy, wy);
         float u, v;
@@ -343,9 +358,15 @@ struct FlowSpline32 {
             if (k != 0.0f) xh = fmaf(-360.0f, k, xh);
         }
         float ft, fx, fy, wx[4], wy[4], dwx[4], dwy[4], r[6];
-        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft);
-        int ix = locate_pair(g.ax[1], xh, ys[0], &fx);
-        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy);
+        bool out = false;
+        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft, &out);
+        int ix = locate_pair(g.ax[1], xh, ys[0], &fx, &out);
+        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy, &out);
+        if (out) {
+            dy[0] = dy[1] = 0.0f;
+            J[0] = J[1] = J[2] = J[3] = 0.0f;
+            return;
+        }
         bspline_w32(fx, wx);
         bspline_w32(fy, wy);
         bspline_dw32(fx, dwx);

@@ -78,8 +78,8 @@ __device__ __forceinline__ void bspline_w64(double t, double* w)
     w[3] = (1.0 / 6.0) * t3 + (0.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
 }
 
-// Cell index and fractional offset along axis d; extrap 0 ("constant")
-// clamps the coordinate into [a, b] first.
+// Cell index and fractional offset along axis d of a coordinate on or inside
+// the grid box (clamped into [a, b]).
 __device__ __forceinline__ int spline_locate64(const SplineGrid& g, int d, int extrap,
                                                double x, double* t)
 {
@@ -102,6 +102,14 @@ __device__ __forceinline__ void spline_eval_uv64(const SplineGrid& g, const doub
                                                  int extrap, double t, double x, double y,
                                                  double* u, double* v)
 {
+    // extrap 0 ("constant", the interpolation package's CONSTANT option): the
+    // interpolant is 0 strictly outside the grid box
+    if (extrap == 0 && (t < g.a[0] || t > g.b[0] || x < g.a[1] || x > g.b[1] || y < g.a[2] ||
+                        y > g.b[2])) {
+        *u = 0.0;
+        *v = 0.0;
+        return;
+    }
     double ft, fx, fy, wt[4], wx[4], wy[4];
     int it = spline_locate64(g, 0, extrap, t, &ft);
     int ix = spline_locate64(g, 1, extrap, x, &fx);

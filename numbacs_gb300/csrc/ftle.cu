@@ -123,6 +123,53 @@ __global__ void ceig_kernel(const double2* __restrict__ F, int nx, int ny, doubl
     }
 }
 
+// C_eig_aux_2D (diagnostics.py:113-197) with utils.gradF_aux_stencil_2D
+// (:50-84) and gradF_main_stencil_2D (:88-124): F is (nx, ny, na, 2).
+// eig_main (na = 5): eigenvectors from the aux-particle tensor, eigenvalues
+// from the main-grid tensor of the centre particles, for 2 <= i < nx-2,
+// 2 <= j < ny-2; otherwise (na = 4) both from the aux tensor, 1-wide border.
+__global__ void ceig_aux_kernel(const double2* __restrict__ F, int nx, int ny, int eig_main,
+                                double dx, double dy, double h, const uint8_t* __restrict__ mask,
+                                double2* __restrict__ evals, double2* __restrict__ evecs)
+{
+    const long n = (long)nx * ny;
+    const int na = eig_main ? 5 : 4, b = eig_main ? 2 : 1;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(k / ny), j = (int)(k - (long)i * ny);
+        double2 ev = make_double2(0.0, 0.0);
+        double2 v0 = make_double2(0.0, 0.0), v1 = make_double2(0.0, 0.0);
+        if (i >= b && i < nx - b && j >= b && j < ny - b && !(mask && mask[k])) {
+            const double2* A = F + k * na;
+            double dxdx = (A[0].x - A[1].x) / (2.0 * h);
+            double dxdy = (A[2].x - A[3].x) / (2.0 * h);
+            double dydx = (A[0].y - A[1].y) / (2.0 * h);
+            double dydy = (A[2].y - A[3].y) / (2.0 * h);
+            double off = dxdx * dxdy + dydx * dydy;
+            double l0, l1, vx, vy;
+            sym2_eig(dxdx * dxdx + dydx * dydx, off, dxdy * dxdy + dydy * dydy, &l0, &l1, &vx, &vy);
+            if (eig_main) {
+                const double2 xp = F[(k + ny) * na + 4], xm = F[(k - ny) * na + 4];
+                const double2 yp = F[(k + 1) * na + 4], ym = F[(k - 1) * na + 4];
+                double mxdx = (xp.x - xm.x) / (2.0 * dx);
+                double mxdy = (yp.x - ym.x) / (2.0 * dy);
+                double mydx = (xp.y - xm.y) / (2.0 * dx);
+                double mydy = (yp.y - ym.y) / (2.0 * dy);
+                double moff = mxdx * mxdy + mydx * mydy;
+                double wx, wy;
+                sym2_eig(mxdx * mxdx + mydx * mydx, moff, mxdy * mxdy + mydy * mydy, &l0, &l1,
+                         &wx, &wy);
+            }
+            ev = make_double2(l0, l1);
+            v0 = make_double2(-vy, vx);
+            v1 = make_double2(vx, vy);
+        }
+        evals[k] = ev;
+        evecs[2 * k] = v0;
+        evecs[2 * k + 1] = v1;
+    }
+}
+
 __global__ void ftle_evec_kernel(const double2* __restrict__ F, int nx, int ny, double den,
                                  double dx, double dy, const uint8_t* __restrict__ mask,
                                  double* __restrict__ ftle, double2* __restrict__ evec)
@@ -246,6 +293,24 @@ extern "C" int nbcs_c_eig_2d(const double* flowmap, int32_t nx, int32_t ny, doub
         return set_error(NBCS_ERR_INVALID, "evals/evecs NULL or not 16-byte aligned");
     ceig_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
         reinterpret_cast<const double2*>(flowmap), nx, ny, dx, dy, mask,
+        reinterpret_cast<double2*>(evals), reinterpret_cast<double2*>(evecs));
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_c_eig_aux_2d(const double* flowmap_aux, int32_t nx, int32_t ny,
+                                 int32_t eig_main, double dx, double dy, double h,
+                                 const uint8_t* mask, double* evals, double* evecs, void* stream)
+{
+    if (nx < 0 || ny < 0) return set_error(NBCS_ERR_INVALID, "c_eig_aux: negative grid size");
+    long n = (long)nx * ny;
+    if (n == 0) return NBCS_OK;
+    if (!flowmap_aux || !evals || !evecs ||
+        ((reinterpret_cast<uintptr_t>(flowmap_aux) | reinterpret_cast<uintptr_t>(evals) |
+          reinterpret_cast<uintptr_t>(evecs)) & 15))
+        return set_error(NBCS_ERR_INVALID, "c_eig_aux: NULL or misaligned array");
+    ceig_aux_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(flowmap_aux), nx, ny, eig_main ? 1 : 0, dx, dy, h, mask,
         reinterpret_cast<double2*>(evals), reinterpret_cast<double2*>(evecs));
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;

@@ -1,7 +1,7 @@
 """FTLE diagnostics: the drop-in for the FTLE part of numbacs.diagnostics.
 
-Reference: src/numbacs/diagnostics.py:21-65 (ftle_grid_2D), :200-244
-(C_eig_2D) and :247-269 (ftle_from_eig).  Each is one fused stencil kernel
+Reference: src/numbacs/diagnostics.py:21-65 (ftle_grid_2D), :113-197
+(C_eig_aux_2D), :200-244 (C_eig_2D) and :247-269 (ftle_from_eig).  Each is one fused stencil kernel
 (csrc/ftle.cu).  ``ftle_evec_2D`` is the fused form of the reference idiom
 ``C_eig_2D`` -> ``ftle_from_eig(eigvals[...,1], T)`` / ``eigvecs[...,:,1]`` that
 feeds ridge extraction.
@@ -75,3 +75,25 @@ def ftle_evec_2D(flowmap, T, dx, dy, mask=None):
     _lib.check(_lib.load().nbcs_ftle_evec_2d(D.ptr(F), nx, ny, float(T), float(dx), float(dy),
                                              D.ptr(md), D.ptr(f), D.ptr(v), D.stream_ptr()))
     return D.finish(f, as_torch), D.finish(v, as_torch)
+
+
+def C_eig_aux_2D(flowmap_aux, dx, dy, h=1e-5, eig_main=True, mask=None):
+    """Cauchy-Green eigenvalues (nx, ny, 2) and eigenvectors (nx, ny, 2, 2) from
+    the auxiliary-grid flow map of flowmap_aux_grid_2D (diagnostics.py:113-197):
+    with ``eig_main`` eigenvectors from the +-h particle differences and
+    eigenvalues from the centre particles' main-grid differences, else both
+    from the +-h differences."""
+    D.require_cuda()
+    as_torch = D.is_torch(flowmap_aux)
+    F = D.to_dev(flowmap_aux)
+    na = 5 if eig_main else 4
+    if F.dim() != 4 or F.shape[2] != na or F.shape[3] != 2:
+        raise ValueError("flowmap_aux must have shape (nx, ny, %d, 2)" % na)
+    nx, ny = int(F.shape[0]), int(F.shape[1])
+    md = D.mask_to_dev(mask)
+    ev = D.empty((nx, ny, 2))
+    vec = D.empty((nx, ny, 2, 2))
+    _lib.check(_lib.load().nbcs_c_eig_aux_2d(D.ptr(F), nx, ny, int(bool(eig_main)), float(dx),
+                                             float(dy), float(h), D.ptr(md), D.ptr(ev),
+                                             D.ptr(vec), D.stream_ptr()))
+    return D.finish(ev, as_torch), D.finish(vec, as_torch)

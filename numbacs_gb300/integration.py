@@ -1,11 +1,14 @@
-"""Flow-map integration: the drop-in for numbacs.integration.flowmap_grid_2D.
+"""Flow-map integration: the drop-in for numbacs.integration.flowmap_grid_2D,
+flowmap_aux_grid_2D and the flow-map composition functions.
 
-Reference: src/numbacs/integration.py:123-182.  The reference loops over the
-particle grid with numba ``prange`` and calls numbalsoda's DOP853 per particle;
-here one CUDA thread integrates one particle (kernels in csrc/flowmap64.cu and
-csrc/flowmap32.cu).  Solver time runs over ``params[0] * [t0, t0 + T]`` and the
-right-hand side is evaluated at ``params[0] * t`` and multiplied by
-``params[0]``, exactly as in the reference.
+Reference: src/numbacs/integration.py:123-182 (flowmap_grid_2D), :249-464
+(flowmap_aux_grid_2D), :609-737 (flowmap_composition, _initial, _step).  The
+reference loops over the particle grid with numba ``prange`` and calls
+numbalsoda's DOP853 per particle; here one CUDA thread (or lane group)
+integrates one particle (kernels in csrc/flowmap64.cu and csrc/flowmap32.cu).
+Solver time runs over ``params[0] * [t0, t0 + T]`` and the right-hand side is
+evaluated at ``params[0] * t`` and multiplied by ``params[0]``, exactly as in
+the reference.  Composition is one gather kernel (csrc/compose.cu).
 """
 import warnings
 
@@ -18,6 +21,16 @@ from .flows import _check_callable_flow
 
 _PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
 STATUS_NAMES = {0: "ok", 1: "masked", -2: "max_steps", -3: "step_underflow", -4: "nonfinite"}
+
+
+def _warn_unfinished(name, status):
+    bad = status[(status != 0) & (status != 1)]
+    if bad.numel():
+        vals, counts = torch.unique(bad, return_counts=True)
+        msg = ", ".join("%s: %d" % (STATUS_NAMES.get(int(v), int(v)), int(c))
+                        for v, c in zip(vals.tolist(), counts.tolist()))
+        warnings.warn("%s: %d particles did not finish (%s)" % (name, bad.numel(), msg),
+                      RuntimeWarning, stacklevel=3)
 
 
 def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, atol=1e-8,
@@ -80,16 +93,127 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
                                       float(atol), D.ptr(md), D.ptr(out), D.ptr(status), opts,
                                       D.stream_ptr()))
     if not return_status and not as_torch:  # torch callers stay asynchronous
-        bad = status[(status != 0) & (status != 1)]
-        if bad.numel():
-            vals, counts = torch.unique(bad, return_counts=True)
-            msg = ", ".join("%s: %d" % (STATUS_NAMES.get(int(v), int(v)), int(c))
-                            for v, c in zip(vals.tolist(), counts.tolist()))
-            warnings.warn("flowmap_grid_2D: %d particles did not finish (%s)" % (bad.numel(), msg),
-                          RuntimeWarning, stacklevel=2)
+        _warn_unfinished("flowmap_grid_2D", status)
     res = [D.finish(out, as_torch)]
     if return_status:
         res.append(D.finish(status, as_torch))
     if return_stats:
         res.append(D.finish(stats, as_torch))
     return res[0] if len(res) == 1 else tuple(res)
+
+
+def flowmap_aux_grid_2D(funcptr, t0, T, x, y, params, h=1e-5, eig_main=True, compute_edge=True,
+                        method="dop853", rtol=1e-6, atol=1e-8, mask=None, *, precision="fp64",
+                        max_steps=100000, return_status=False):
+    """Flow map of the auxiliary grid (x_i, y_j) + (+-h, 0), (0, +-h) [, (0, 0)]
+    -> (nx, ny, 5, 2) with ``eig_main`` (the last particle is the grid point
+    itself), else (nx, ny, 4, 2).
+
+    Same positional signature, defaults and skip rules as the reference
+    (integration.py:249-464): with ``compute_edge`` the edge points integrate
+    only their centre particle (eig_main) or all four; without it they are
+    left 0.  Masked points are left 0.  ``precision="mixed"`` is accepted, but
+    C_eig_aux_2D divides differences of trajectories 2h apart by 2h, which
+    amplifies the FP32 stage rounding about 1/(2h)-fold: the FP64 default is the
+    path for this function.
+    """
+    if method.lower() != "dop853":
+        raise NotImplementedError("method=%r: only 'dop853' is implemented on the GPU" % method)
+    flow = _check_callable_flow(funcptr)
+    if precision not in _PREC:
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    D.require_cuda()
+    as_torch = D.is_torch(x, y)
+    xd, yd = D.to_dev(x), D.to_dev(y)
+    nx, ny = xd.numel(), yd.numel()
+    na = 5 if eig_main else 4
+    md = D.mask_to_dev(mask)
+    if md is not None and tuple(md.shape) != (nx, ny):
+        raise ValueError("mask must have shape (nx, ny)")
+    prm = np.ascontiguousarray(
+        params.cpu().numpy() if isinstance(params, torch.Tensor) else params, dtype=np.float64)
+    out = D.empty((nx, ny, na, 2))
+    status = D.empty((nx, ny, na), torch.int32)
+    opts = _lib.NbcsOpts()
+    opts.precision = _PREC[precision]
+    opts.max_steps = int(max_steps)
+    _lib.check(_lib.load().nbcs_flowmap_aux_grid_2d(
+        flow.struct, float(t0), float(T), D.ptr(xd), nx, D.ptr(yd), ny,
+        prm.ctypes.data_as(_lib._vp), len(prm), float(h), int(bool(eig_main)),
+        int(bool(compute_edge)), float(rtol), float(atol), D.ptr(md), D.ptr(out), D.ptr(status),
+        opts, D.stream_ptr()))
+    if not return_status and not as_torch:
+        _warn_unfinished("flowmap_aux_grid_2D", status)
+    if return_status:
+        return D.finish(out, as_torch), D.finish(status, as_torch)
+    return D.finish(out, as_torch)
+
+
+def UCGrid(*axes):
+    """The interpolation package's uniform Cartesian grid: a tuple of
+    (a, b, n) per axis, n an int (what the reference's tests build with
+    ``interpolation.splines.UCGrid``)."""
+    return tuple((float(a), float(b), int(n)) for a, b, n in axes)
+
+
+def _grid6(grid, nx, ny):
+    (x0, x1, gnx), (y0, y1, gny) = grid
+    if (int(gnx), int(gny)) != (nx, ny):
+        raise ValueError("grid has %s x %s points, the flow maps %d x %d" % (gnx, gny, nx, ny))
+    return np.array([x0, x1, gnx, y0, y1, gny], np.float64)
+
+
+def flowmap_composition(flowmaps, grid, nT, *, first=0):
+    """Composed flow map (nx, ny, 2) of the nT maps ``flowmaps`` (nT, nx, ny, 2)
+    (integration.py:609-641): the points start at the first map, pass through
+    the next ones by bilinear interpolation on ``grid`` (0 outside it, the
+    interpolation package's CONSTANT extrapolation) and end at the last.
+
+    Keyword-only extra: ``first`` reads the stack as a ring buffer, map j of
+    the sequence being ``flowmaps[(first + j) % nT]``, so a time series can
+    overwrite its oldest map instead of shifting the stack.
+    """
+    D.require_cuda()
+    as_torch = D.is_torch(flowmaps)
+    F = D.to_dev(flowmaps)
+    nT = int(nT)
+    if F.dim() != 4 or F.shape[3] != 2 or F.shape[0] != nT:
+        raise ValueError("flowmaps must have shape (nT, nx, ny, 2)")
+    nx, ny = int(F.shape[1]), int(F.shape[2])
+    g = _grid6(grid, nx, ny)
+    out = D.empty((nx, ny, 2))
+    _lib.check(_lib.load().nbcs_flowmap_compose(D.ptr(F), nT, int(first) % nT,
+                                                g.ctypes.data_as(_lib._vp), D.ptr(out),
+                                                D.stream_ptr()))
+    return D.finish(out, as_torch)
+
+
+def flowmap_composition_initial(funcptr, t0, T, h, x, y, grid, params, **kwargs):
+    """integration.py:644-685: the nT = |round(T / h)| flow maps over
+    [t0 + k h, t0 + (k + 1) h] and their composition -> (flowmap0, flowmaps, nT).
+    ``kwargs`` go to flowmap_grid_2D."""
+    D.require_cuda()
+    as_torch = D.is_torch(x, y)
+    xd, yd = D.to_dev(x), D.to_dev(y)
+    nT = abs(round(T / h))
+    fms = D.empty((nT, xd.numel(), yd.numel(), 2))
+    for k in range(nT):
+        flowmap_grid_2D(funcptr, t0, h, xd, yd, params, out=fms[k], **kwargs)
+        t0 += h
+    fm0 = flowmap_composition(fms, grid, nT)
+    return D.finish(fm0, as_torch), D.finish(fms, as_torch), nT
+
+
+def flowmap_composition_step(flowmaps, funcptr, t0, h, nT, x, y, grid, params, **kwargs):
+    """integration.py:688-737: drop the oldest map, integrate the newest over
+    [t0, t0 + h], compose -> (flowmap_k, flowmaps).  ``flowmaps`` is updated in
+    place (numpy array or CUDA tensor), as in the reference."""
+    D.require_cuda()
+    if isinstance(flowmaps, torch.Tensor) and flowmaps.is_cuda:
+        flowmaps[:-1] = flowmaps[1:].clone()
+        flowmap_grid_2D(funcptr, t0, h, D.to_dev(x), D.to_dev(y), params, out=flowmaps[-1],
+                        **kwargs)
+        return flowmap_composition(flowmaps, grid, nT), flowmaps
+    flowmaps[:-1] = flowmaps[1:]
+    flowmaps[-1] = flowmap_grid_2D(funcptr, t0, h, x, y, params, **kwargs)
+    return flowmap_composition(flowmaps, grid, nT), flowmaps

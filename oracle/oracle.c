@@ -90,8 +90,9 @@ static void bspline_weights(double t, double w[4])
     w[3] = (1.0 / 6.0) * t3 + (0.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
 }
 
-/* cell index and fractional offset along one axis (a, b, n); extrap 0
- * clamps the coordinate into [a, b] first */
+/* cell index and fractional offset along one axis (a, b, n); the coordinate
+ * is clamped into [a, b] (only points on or inside the box get here when
+ * extrap is 0) */
 static int spline_locate(double a, double b, int n, int extrap, double x, double* t)
 {
     if (extrap == 0) {
@@ -114,6 +115,13 @@ double orc_eval_spline_3d(const double* g, const double* c, int extrap,
 {
     int nt = (int)g[2], nx = (int)g[5], ny = (int)g[8];
     int sx = ny + 2, st = (nx + 2) * (ny + 2);
+    /* extrap 0 ("constant", the interpolation package's CONSTANT option): the
+     * interpolant is 0 strictly outside the grid box.  Pinned through
+     * flowmap_composition's fixtures (integration.py:630-640 evaluate
+     * eval_linear(..., xto.CONSTANT); wall points that a map leaves 1 ulp
+     * outside [0, 2] compose to 0 there); eval_spline takes the same option. */
+    if (extrap == 0 && (t < g[0] || t > g[1] || x < g[3] || x > g[4] || y < g[6] || y > g[7]))
+        return 0.0;
     double ft, fx, fy, wt[4], wx[4], wy[4];
     int it = spline_locate(g[0], g[1], nt, extrap, t, &ft);
     int ix = spline_locate(g[3], g[4], nx, extrap, x, &fx);
@@ -637,5 +645,173 @@ void orc_ridge_field(const double* f, const double* ev, const double* x, int nx,
                 }
             }
         }
+    }
+}
+
+/* ------------------------------------------------------ auxiliary grid */
+
+/* Which particles flowmap_aux_grid_2D integrates (integration.py:320-464,
+ * method "dop853"): with eig_main (n_aux = 5) an edge point integrates only
+ * its centre particle (k = 4) when compute_edge is set; without eig_main
+ * (n_aux = 4) every point integrates all four when compute_edge is set; with
+ * compute_edge off the edge points are skipped. */
+static int aux_active(int i, int j, int k, int nx, int ny, int n_aux, int compute_edge)
+{
+    const int edge = (i == 0 || i == nx - 1 || j == 0 || j == ny - 1);
+    if (!edge) return 1;
+    if (!compute_edge) return 0;
+    return n_aux == 4 || k == 4;
+}
+
+/* integration.py:249-464: particle k of grid point (i, j) starts at
+ * (x_i, y_j) + aux_k with aux = (h,0), (-h,0), (0,h), (0,-h) [, (0,0)];
+ * out (nx,ny,n_aux,2); masked and skipped entries stay 0 (status MASKED). */
+int orc_flowmap_aux_grid_2d(const orc_flow* fl, double t0, double T, const double* x, int nx,
+                            const double* y, int ny, const double* params, double h,
+                            int eig_main, int compute_edge, double rtol, double atol,
+                            const uint8_t* mask, double* out, int32_t* status, int32_t* stats,
+                            int nmax, int nthreads)
+{
+    const int n_aux = eig_main ? 5 : 4;
+    const double aux[5][2] = {{h, 0.0}, {-h, 0.0}, {0.0, h}, {0.0, -h}, {0.0, 0.0}};
+    double ts = params[0] * t0;
+    double te = params[0] * (t0 + T);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int i = 0; i < nx; ++i) {
+        for (int j = 0; j < ny; ++j) {
+            for (int k = 0; k < n_aux; ++k) {
+                size_t q = ((size_t)i * ny + j) * n_aux + k;
+                if ((mask && mask[(size_t)i * ny + j]) || !aux_active(i, j, k, nx, ny, n_aux, compute_edge)) {
+                    out[2 * q] = 0.0;
+                    out[2 * q + 1] = 0.0;
+                    if (status) status[q] = ORC_MASKED;
+                    if (stats) { stats[3 * q] = 0; stats[3 * q + 1] = 0; stats[3 * q + 2] = 0; }
+                    continue;
+                }
+                double yv[2] = {x[i] + aux[k][0], y[j] + aux[k][1]};
+                int st = orc_dop853(fl, params, ts, te, yv, rtol, atol, nmax, stats ? stats + 3 * q : 0);
+                out[2 * q] = yv[0];
+                out[2 * q + 1] = yv[1];
+                if (status) status[q] = st;
+            }
+        }
+    }
+    return 0;
+}
+
+/* diagnostics.py:113-197 (C_eig_aux_2D) with utils.gradF_aux_stencil_2D
+ * (:50-84) and gradF_main_stencil_2D (:88-124).  eig_main: eigenvectors from
+ * the aux-grid tensor, eigenvalues from the main-grid tensor (centre
+ * particles, spacing dx, dy), for 2 <= i < nx-2, 2 <= j < ny-2; otherwise both
+ * from the aux-grid tensor for 1 <= i < nx-1, 1 <= j < ny-1. */
+void orc_c_eig_aux_2d(const double* F, int nx, int ny, double dx, double dy, double h,
+                      int eig_main, const uint8_t* mask, double* evals, double* evecs)
+{
+    const int n_aux = eig_main ? 5 : 4, b = eig_main ? 2 : 1;
+    memset(evals, 0, sizeof(double) * (size_t)nx * ny * 2);
+    memset(evecs, 0, sizeof(double) * (size_t)nx * ny * 4);
+#ifdef _OPENMP
+#pragma omp parallel for
+#endif
+    for (int i = b; i < nx - b; ++i) {
+        for (int j = b; j < ny - b; ++j) {
+            size_t k = (size_t)i * ny + j;
+            if (mask && mask[k]) continue;
+            const double* A = F + 2 * n_aux * k;  /* A[2*m + c]: particle m, component c */
+            double dxdx = (A[0] - A[2]) / (2.0 * h);
+            double dxdy = (A[4] - A[6]) / (2.0 * h);
+            double dydx = (A[1] - A[3]) / (2.0 * h);
+            double dydy = (A[5] - A[7]) / (2.0 * h);
+            double off = dxdx * dxdy + dydx * dydy;
+            double l0, l1, vx, vy;
+            sym2_eig(dxdx * dxdx + dydx * dydx, off, dxdy * dxdy + dydy * dydy, &l0, &l1, &vx, &vy);
+            if (eig_main) {
+                const int c = 2 * (n_aux - 1);  /* centre particle */
+                const double* xp = F + 2 * n_aux * (k + ny) + c;
+                const double* xm = F + 2 * n_aux * (k - ny) + c;
+                const double* yp = F + 2 * n_aux * (k + 1) + c;
+                const double* ym = F + 2 * n_aux * (k - 1) + c;
+                double mxdx = (xp[0] - xm[0]) / (2.0 * dx);
+                double mxdy = (yp[0] - ym[0]) / (2.0 * dy);
+                double mydx = (xp[1] - xm[1]) / (2.0 * dx);
+                double mydy = (yp[1] - ym[1]) / (2.0 * dy);
+                double moff = mxdx * mxdy + mydx * mydy;
+                double wx, wy;
+                sym2_eig(mxdx * mxdx + mydx * mydx, moff, mxdy * mxdy + mydy * mydy, &l0, &l1,
+                         &wx, &wy);
+            }
+            evals[2 * k] = l0;
+            evals[2 * k + 1] = l1;
+            evecs[4 * k + 0] = -vy;
+            evecs[4 * k + 1] = vx;
+            evecs[4 * k + 2] = vx;
+            evecs[4 * k + 3] = vy;
+        }
+    }
+}
+
+/* --------------------------------------------------- flow-map composition */
+
+/* Cell and offset of x on the uniform axis (a, b, n) for multilinear
+ * interpolation of a point inside [a, b]. */
+static int lin_locate(double a, double b, int n, double x, double* lam)
+{
+    if (x != x) { *lam = x; return 0; }
+    if (x < a) x = a;
+    if (x > b) x = b;
+    double d = (b - a) / (double)(n - 1);
+    double u = (x - a) / d;
+    int i = (int)floor(u);
+    if (i > n - 2) i = n - 2;
+    if (i < 0) i = 0;
+    *lam = u - (double)i;
+    return i;
+}
+
+/* eval_linear(grid, f[..., c], (px, py)) on f (nx, ny, 2) */
+static void bilinear2(const double* f, const double* g, int nx, int ny, double px, double py,
+                      double* r)
+{
+    if (px < g[0] || px > g[1] || py < g[3] || py > g[4]) {  /* xto.CONSTANT: 0 outside */
+        r[0] = r[1] = 0.0;
+        return;
+    }
+    double l0, l1;
+    int i = lin_locate(g[0], g[1], nx, px, &l0);
+    int j = lin_locate(g[3], g[4], ny, py, &l1);
+    const double* f00 = f + 2 * ((size_t)i * ny + j);
+    const double* f10 = f00 + 2 * (size_t)ny;
+    for (int c = 0; c < 2; ++c)
+        r[c] = (1.0 - l0) * ((1.0 - l1) * f00[c] + l1 * f00[2 + c])
+             + l0 * ((1.0 - l1) * f10[c] + l1 * f10[2 + c]);
+}
+
+/* integration.py:609-641 (flowmap_composition): the points start at the
+ * first map's values, pass through maps 1 .. nT-2 by bilinear interpolation
+ * on the grid (x0, x1, nx, y0, y1, ny; 0 outside it, xto.CONSTANT) and end
+ * at the last map (nT = 1
+ * therefore interpolates the single map at its own values, as the reference
+ * does).  Map j of the sequence is fms[(first + j) % nT] (a ring buffer). */
+void orc_flowmap_compose(const double* fms, int nT, int first, int nx, int ny, const double* grid,
+                         double* out)
+{
+    const size_t m = (size_t)nx * ny * 2;
+#ifdef _OPENMP
+#pragma omp parallel for
+#endif
+    for (long p = 0; p < (long)nx * ny; ++p) {
+        const double* f0 = fms + m * (size_t)(first % nT);
+        double pt[2] = {f0[2 * p], f0[2 * p + 1]}, r[2];
+        for (int k = 1; k < nT - 1; ++k) {
+            bilinear2(fms + m * (size_t)((first + k) % nT), grid, nx, ny, pt[0], pt[1], r);
+            pt[0] = r[0];
+            pt[1] = r[1];
+        }
+        bilinear2(fms + m * (size_t)((first + nT - 1) % nT), grid, nx, ny, pt[0], pt[1], r);
+        out[2 * p] = r[0];
+        out[2 * p + 1] = r[1];
     }
 }

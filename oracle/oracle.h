@@ -80,6 +80,20 @@ void orc_ridge_field(const double* f, const double* evec, const double* x, int n
                      const double* y, int ny, double sdd_thresh, double f_min,
                      uint8_t* mask_out, double* rpts_full);
 
+/* flowmap_aux_grid_2D: out (nx,ny,n_aux,2), n_aux = 5 (eig_main) or 4 */
+int orc_flowmap_aux_grid_2d(const orc_flow* flow, double t0, double T, const double* x, int nx,
+                            const double* y, int ny, const double* params, double h,
+                            int eig_main, int compute_edge, double rtol, double atol,
+                            const uint8_t* mask, double* out, int32_t* status, int32_t* stats,
+                            int nmax, int nthreads);
+/* C_eig_aux_2D: evals (nx,ny,2), evecs (nx,ny,2,2) */
+void orc_c_eig_aux_2d(const double* fm_aux, int nx, int ny, double dx, double dy, double h,
+                      int eig_main, const uint8_t* mask, double* evals, double* evecs);
+/* flowmap_composition over nT maps (nT,nx,ny,2) read in ring order from `first`;
+ * grid = x0, x1, nx, y0, y1, ny */
+void orc_flowmap_compose(const double* fms, int nT, int first, int nx, int ny,
+                         const double* grid, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,10 @@ def lib():
         L.orc_percentile.argtypes = [vp, i64, d]
         L.orc_percentile.restype = d
         L.orc_ridge_field.argtypes = [vp, vp, vp, i, vp, i, d, d, vp, vp]
+        L.orc_flowmap_aux_grid_2d.argtypes = [vp, d, d, vp, i, vp, i, vp, d, i, i, d, d, vp, vp,
+                                              vp, vp, i, i]
+        L.orc_c_eig_aux_2d.argtypes = [vp, i, i, d, d, d, i, vp, vp, vp]
+        L.orc_flowmap_compose.argtypes = [vp, i, i, i, i, vp, vp]
         for fn in (L.orc_cos_deg, L.orc_root8):
             fn.argtypes = [d]
             fn.restype = d
@@ -167,6 +171,69 @@ def flowmap_grid_2D(flow, t0, T, x, y, params, rtol=1e-6, atol=1e-8, mask=None,
     if return_status:
         return out, status, stats
     return out
+
+
+def flowmap_aux_grid_2D(flow, t0, T, x, y, params, h=1e-5, eig_main=True, compute_edge=True,
+                        rtol=1e-6, atol=1e-8, mask=None, nmax=100000, nthreads=0,
+                        return_status=False):
+    """integration.py:249-464 (method dop853)."""
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    p = np.ascontiguousarray(params, np.float64)
+    nx, ny = len(x), len(y)
+    na = 5 if eig_main else 4
+    out = np.zeros((nx, ny, na, 2))
+    status = np.zeros((nx, ny, na), np.int32)
+    stats = np.zeros((nx, ny, na, 3), np.int32)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib().orc_flowmap_aux_grid_2d(flow.ptr, float(t0), float(T), _dp(x), nx, _dp(y), ny, _dp(p),
+                                  float(h), int(bool(eig_main)), int(bool(compute_edge)),
+                                  float(rtol), float(atol), _dp(m), _dp(out), _dp(status),
+                                  _dp(stats), int(nmax), int(nthreads))
+    if return_status:
+        return out, status, stats
+    return out
+
+
+def C_eig_aux_2D(flowmap_aux, dx, dy, h=1e-5, eig_main=True, mask=None):
+    """diagnostics.py:113-197."""
+    F = np.ascontiguousarray(flowmap_aux, np.float64)
+    nx, ny = F.shape[:2]
+    if F.shape[2] != (5 if eig_main else 4):
+        raise ValueError("flowmap_aux has %d aux particles" % F.shape[2])
+    ev = np.zeros((nx, ny, 2))
+    vec = np.zeros((nx, ny, 2, 2))
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib().orc_c_eig_aux_2d(_dp(F), nx, ny, float(dx), float(dy), float(h), int(bool(eig_main)),
+                           _dp(m), _dp(ev), _dp(vec))
+    return ev, vec
+
+
+def flowmap_composition(flowmaps, grid, nT, first=0):
+    """integration.py:609-641; grid = ((x0, x1, nx), (y0, y1, ny))."""
+    F = np.ascontiguousarray(flowmaps, np.float64)
+    (x0, x1, nx), (y0, y1, ny) = grid
+    g = np.array([x0, x1, nx, y0, y1, ny], np.float64)
+    out = np.zeros((int(nx), int(ny), 2))
+    lib().orc_flowmap_compose(_dp(F), int(nT), int(first), int(nx), int(ny), _dp(g), _dp(out))
+    return out
+
+
+def flowmap_composition_initial(flow, t0, T, h, x, y, grid, params, **kw):
+    """integration.py:644-685."""
+    nT = abs(round(T / h))
+    fms = np.zeros((nT, len(x), len(y), 2))
+    for k in range(nT):
+        fms[k] = flowmap_grid_2D(flow, t0, h, x, y, params, **kw)
+        t0 += h
+    return flowmap_composition(fms, grid, nT), fms, nT
+
+
+def flowmap_composition_step(flowmaps, flow, t0, h, nT, x, y, grid, params, **kw):
+    """integration.py:688-737 (shifts flowmaps in place, as the reference does)."""
+    flowmaps[:-1] = flowmaps[1:].copy()
+    flowmaps[-1] = flowmap_grid_2D(flow, t0, h, x, y, params, **kw)
+    return flowmap_composition(flowmaps, grid, nT), flowmaps
 
 
 def ftle_grid_2D(flowmap, T, dx, dy, mask=None):

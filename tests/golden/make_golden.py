@@ -11,6 +11,14 @@ imported here because numba / numbalsoda / interpolation are absent):
   tests/testing_data/Cevecs.npy
   tests/testing_data/ridge_pts.npy  ftle_ridge_pts(ftle, Cevecs[...,1], x, y) (tests/test_extraction.py:6-12)
   tests/testing_data/ridges.pkl     ftle_ridges(ftle, Cevecs[...,1], x, y)    (tests/test_extraction.py:14-20)
+  tests/testing_data/fm_ci.npy,     flowmap_composition_initial, double gyre 21x11, t0=0, T=8,
+  tests/testing_data/fms_ci.npy     h=1 (nT=8)                     (tests/test_integration.py:92-103)
+  tests/testing_data/fm_cs.npy,     flowmap_composition_step from fms_ci at t0=8
+  tests/testing_data/fms_cs.npy                                    (tests/test_integration.py:105-114)
+  tests/testing_data/fm_aux.npy     flowmap_aux_grid_2D, double gyre 21x11, t0=0, T=8, h=1e-5
+                                    (tests/test_integration.py:66-75)
+  tests/testing_data/Cevals_aux.npy, C_eig_aux_2D(fm_aux, 0.1, 0.1)  (tests/test_diagnostics.py:112-131)
+  tests/testing_data/Cevecs_aux.npy
   tests/test_flows.py literals      spline coefficients Cu/Cv (:74-133), spline values at 27
                                     points (:208-229), double-gyre and Bickley velocities
                                     at the same 27 points (:315-357)
@@ -83,7 +91,8 @@ def _test_literals(path):
 def main(ref_root):
     td = os.path.join(ref_root, "tests", "testing_data")
     arrays = {}
-    for name in ("fm", "ftle", "Cevals", "Cevecs", "ridge_pts"):
+    for name in ("fm", "ftle", "Cevals", "Cevecs", "ridge_pts", "fm_ci", "fms_ci", "fm_cs",
+                 "fms_cs", "fm_aux", "Cevals_aux", "Cevecs_aux"):
         arrays[name] = np.load(os.path.join(td, name + ".npy"), allow_pickle=False)
     ridges = _load_pkl(os.path.join(td, "ridges.pkl"))
     arrays["n_ridges"] = np.array(len(ridges))

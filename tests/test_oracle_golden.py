@@ -117,8 +117,103 @@ def test_deterministic_math_accuracy(orc):
 
 
 def test_extrapolation_is_constant(orc):
-    # extrap_mode="constant": outside the grid box the value on its boundary
+    # extrap_mode="constant" (the interpolation package's CONSTANT option): 0
+    # strictly outside the grid box, the spline's value on it
     t, xs, u, v, pts = _spline_case()
     grid, Cu, _ = orc.get_interp_arrays_2D(t, xs, xs, u, v)
-    inside = orc.eval_spline_3d(grid, Cu, 0.2, 1.0, 0.3)
-    assert orc.eval_spline_3d(grid, Cu, 0.7, 5.0, 0.3) == inside
+    (t0, t1, _), (x0, x1, _), (y0, y1, _) = grid
+    on_edge = orc.eval_spline_3d(grid, Cu, t0, x1, y0)
+    assert on_edge != 0.0
+    assert orc.eval_spline_3d(grid, Cu, t0, np.nextafter(x1, 2 * x1), y0) == 0.0
+    assert orc.eval_spline_3d(grid, Cu, np.nextafter(t0, -1.0), x0, y0) == 0.0
+    assert orc.eval_spline_3d(grid, Cu, 0.5 * (t0 + t1), 0.5 * (x0 + x1), y1 + 1.0) == 0.0
+
+
+GRID_DG = ((0.0, 2.0, 21), (0.0, 1.0, 11))
+
+
+def test_flowmap_composition_initial(orc, golden, coords_dg):
+    """tests/test_integration.py:92-103: double gyre, t0 = 0, T = 8, h = 1 -> nT = 8."""
+    x, y = coords_dg
+    p = orc.double_gyre_params(1.0)
+    fm0, fms, nT = orc.flowmap_composition_initial(orc.double_gyre(), 0.0, T_FIX, 1.0, x, y,
+                                                   GRID_DG, p)
+    assert nT == 8
+    assert np.allclose(fms.astype(np.float32), golden["fms_ci"])
+    assert np.allclose(fm0.astype(np.float32), golden["fm_ci"])
+
+
+def test_flowmap_composition_step(orc, golden, coords_dg):
+    """tests/test_integration.py:105-114: one step from the float32 fixture maps at t0 = 8."""
+    x, y = coords_dg
+    p = orc.double_gyre_params(1.0)
+    fms = golden["fms_ci"].astype(np.float64)
+    fmk, fms2 = orc.flowmap_composition_step(fms, orc.double_gyre(), T_FIX, 1.0, 8, x, y,
+                                             GRID_DG, p)
+    assert np.allclose(fmk.astype(np.float32), golden["fm_cs"])
+    assert np.allclose(fms2.astype(np.float32), golden["fms_cs"])
+
+
+def test_flowmap_composition_ring_order_and_nT1(orc, golden):
+    """Ring order (first = r) equals composing the rolled stack; nT = 1 composes the
+    single map with itself, as integration.py:630-640 does."""
+    fms = golden["fms_ci"].astype(np.float64)
+    ref = orc.flowmap_composition(fms, GRID_DG, 8)
+    for r in (1, 3, 7):
+        ring = np.roll(fms, r, axis=0)  # map j of the sequence sits at index (j + r) % 8
+        assert np.array_equal(orc.flowmap_composition(ring, GRID_DG, 8, first=r), ref)
+    one = orc.flowmap_composition(fms[:1], GRID_DG, 1)
+    two = orc.flowmap_composition(np.stack([fms[0], fms[0]]), GRID_DG, 2)
+    assert np.array_equal(one, two)
+
+
+def test_flowmap_aux_grid_2D(orc, golden, coords_dg, mask_dg):
+    """tests/test_integration.py:66-75."""
+    x, y = coords_dg
+    p = orc.double_gyre_params(1.0)
+    fa, st, _ = orc.flowmap_aux_grid_2D(orc.double_gyre(), 0.0, T_FIX, x, y, p, return_status=True)
+    assert fa.shape == (21, 11, 5, 2)
+    assert np.allclose(fa.astype(np.float32), golden["fm_aux"])
+    # edge points integrate their centre particle only; interior points all five
+    edge = np.zeros((21, 11), bool)
+    edge[[0, -1], :] = True
+    edge[:, [0, -1]] = True
+    assert (st[edge][:, :4] == 1).all() and (st[edge][:, 4] == 0).all()
+    assert (st[~edge] == 0).all()
+    # the centre particles are the plain flow map
+    fm = orc.flowmap_grid_2D(orc.double_gyre(), 0.0, T_FIX, x, y, p)
+    assert np.array_equal(fa[:, :, 4], fm)
+    fam = orc.flowmap_aux_grid_2D(orc.double_gyre(), 0.0, T_FIX, x, y, p, mask=mask_dg)
+    assert np.allclose(fam.astype(np.float32), apply_mask(golden["fm_aux"], mask_dg))
+
+
+def test_flowmap_aux_grid_2D_variants(orc, coords_dg):
+    """eig_main=False (4 aux particles) and compute_edge=False skip rules
+    (integration.py:320-464)."""
+    x, y = coords_dg
+    p = orc.double_gyre_params(1.0)
+    f4, s4, _ = orc.flowmap_aux_grid_2D(orc.double_gyre(), 0.0, 2.0, x, y, p, eig_main=False,
+                                        return_status=True)
+    assert f4.shape == (21, 11, 4, 2) and (s4 == 0).all()
+    f5 = orc.flowmap_aux_grid_2D(orc.double_gyre(), 0.0, 2.0, x, y, p)
+    assert np.array_equal(f4[1:-1, 1:-1], f5[1:-1, 1:-1, :4])
+    fn, sn, _ = orc.flowmap_aux_grid_2D(orc.double_gyre(), 0.0, 2.0, x, y, p, compute_edge=False,
+                                        return_status=True)
+    assert (sn[[0, -1]] == 1).all() and (sn[:, [0, -1]] == 1).all()
+    assert (fn[[0, -1]] == 0).all() and (fn[:, [0, -1]] == 0).all()
+    assert np.array_equal(fn[1:-1, 1:-1], f5[1:-1, 1:-1])
+
+
+def test_C_eig_aux_2D(orc, golden, mask_dg):
+    """tests/test_diagnostics.py:112-131 (fed the float32 fixture, as there)."""
+    fa = golden["fm_aux"].astype(np.float64)
+    ev, vec = orc.C_eig_aux_2D(fa, 0.1, 0.1)
+    C_exp = reconstruct(golden["Cevals_aux"], golden["Cevecs_aux"])
+    assert np.allclose(reconstruct(ev.astype(np.float32), vec.astype(np.float32)), C_exp)
+    evm, vecm = orc.C_eig_aux_2D(fa, 0.1, 0.1, mask=mask_dg)
+    assert np.allclose(reconstruct(evm.astype(np.float32), vecm.astype(np.float32)),
+                       apply_mask(C_exp, mask_dg))
+    # eig_main=False: both from the aux stencil, over the 1-wide interior
+    ev4, vec4 = orc.C_eig_aux_2D(fa[:, :, :4], 0.1, 0.1, eig_main=False)
+    assert np.array_equal(vec4[2:-2, 2:-2], vec[2:-2, 2:-2])
+    assert (ev4[1:-1, 1:-1, 1] > 0).all()
