@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched time-series leg")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the composition / auxiliary-grid measurements")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned step proposer")
     ap.add_argument("--sweep", action="store_true",
                     help="precision sweep (double gyre / geo 0.05 deg, rtol 1e-5..1e-8) only")
@@ -67,6 +69,9 @@ def parse():
     ap.add_argument("--lanes", type=int, default=None,
                     help="fixed lanes per particle (with --blocks-per-sm: skips the autotuner)")
     ap.add_argument("--blocks-per-sm", type=int, default=None)
+    ap.add_argument("--kernel-case", default=None,
+                    choices=["ftle", "ridge", "compose", "label", "batch", "mlp"],
+                    help="run one small case of one kernel family 3 times (for ncu captures)")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no ladder, plain comparison, e2e or CPU baseline)")
     return ap.parse_args()
@@ -425,6 +430,8 @@ def run_ours(args, rank, world):
     }
     if not args.quick and not args.no_batch:
         out["batch"] = run_batch(wl, rtol, max(2, min(args.steps, 5)))
+    if not args.quick and not args.no_rows:
+        out["composition"], out["aux_grid"] = run_rows(wl, rtol)
     if not args.no_e2e and not args.quick:
         out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
     if not args.no_cpu_baseline and not args.quick and rank == 0:
@@ -485,7 +492,7 @@ def run_batch(wl, rtol, steps):
             "launch": "one integrator launch + one FTLE launch, CUDA graph replay"}
 
 
-def train_proposer(rtol, atol, seeds=range(8), t0s=(168.0, 190.0, 215.0), sample=0.15):
+def train_proposer(rtol, atol, seeds=range(8), t0s=(168.0, 190.0, 215.0), sample=0.22):
     """Step-size MLP trained on steps logged by the integrator on the synthetic
     geophysical flows of `seeds` (0.4 deg particle grids, T = -72 h)."""
     import torch
@@ -657,6 +664,76 @@ def _profile_traffic(prec):
     return None
 
 
+def _hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh).get("hbm_gbs")
+    except (OSError, ValueError):
+        return None
+
+
+def run_rows(wl, rtol, nT=72):
+    """Flow-map composition and the auxiliary grid on the headline workload.
+
+    Composition: nT = 72 one-hour maps of the 676 x 251 particle grid (mixed
+    path, t0 = 180 h, backward), composed into the 72 h map; one composition
+    gathers a 2 x 2 cell of double2 per map per particle (64 B) plus the first
+    map and the output (16 B each); the 196 MB stack exceeds L2, L2 is flushed
+    before each timed call.  Auxiliary grid: flowmap_aux_grid_2D (FP64, h =
+    1e-5, 5 particles per point) of the same grid, T = -72 h, then C_eig_aux_2D.
+    """
+    import torch
+    import numbacs_gb300 as nb
+    x = torch.from_numpy(wl["lonf"]).cuda()
+    y = torch.from_numpy(wl["latf"]).cuda()
+    nx, ny = x.numel(), y.numel()
+    grid = nb.UCGrid((wl["lonf"][0], wl["lonf"][-1], nx), (wl["latf"][0], wl["latf"][-1], ny))
+    fms = torch.empty((nT, nx, ny, 2), dtype=torch.float64, device="cuda")
+    t = wl["t0"]
+    for k in range(nT):
+        nb.flowmap_grid_2D(wl["flow"], t, -1.0, x, y, wl["params"], rtol=rtol, atol=1e-2 * rtol,
+                           precision="mixed", out=fms[k])
+        t -= 1.0
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nb.flowmap_composition(fms, grid, nT)
+    times = []
+    for _ in range(5):
+        flush.zero_()
+        a.record()
+        nb.flowmap_composition(fms, grid, nT)
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = min(times)
+    byts = nx * ny * (16 + 64 * (nT - 1) + 16)
+    peak = _hbm_peak()
+    comp = {"maps": nT, "grid": [nx, ny], "ms": ms, "particles_per_s": nx * ny / (ms * 1e-3),
+            "algorithmic_bytes": byts, "achieved_gbs": byts / (ms * 1e-3) / 1e9,
+            "hbm_peak_gbs_measured": peak,
+            "frac": (byts / (ms * 1e-3) / 1e9) / peak if peak else None,
+            "note": "gathers of neighbouring particles share sectors: DRAM traffic is below the "
+                    "algorithmic bytes"}
+    fa = nb.flowmap_aux_grid_2D(wl["flow"], wl["t0"], wl["T"], x, y, wl["params"], rtol=rtol,
+                                atol=1e-2 * rtol)
+    torch.cuda.synchronize()
+    a.record()
+    fa = nb.flowmap_aux_grid_2D(wl["flow"], wl["t0"], wl["T"], x, y, wl["params"], rtol=rtol,
+                                atol=1e-2 * rtol)
+    b.record()
+    torch.cuda.synchronize()
+    ms_aux = a.elapsed_time(b)
+    a.record()
+    nb.C_eig_aux_2D(fa, wl["dx"], wl["dy"])
+    b.record()
+    torch.cuda.synchronize()
+    n_aux = nx * ny * 5 - 4 * 2 * (nx + ny - 2)  # edge points integrate their centre only
+    aux = {"grid": [nx, ny], "precision": "fp64", "rtol": rtol, "h": 1e-5,
+           "particles": n_aux, "ms": ms_aux, "particles_per_s": n_aux / (ms_aux * 1e-3),
+           "c_eig_aux_ms": a.elapsed_time(b)}
+    return comp, aux
+
+
 def run_e2e(nb, D, wl, prec, rtol, atol, args, world):
     """Same step through the public numpy API: host arrays in, host results out."""
     import torch
@@ -774,8 +851,75 @@ def run_reference(args, rank, world):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_kernel_case(name, reps=3):
+    """One kernel family on a case sized for an ncu capture (inputs above L2
+    where the kernel is HBM-bound), launched `reps` times; returns CUDA-event
+    times.  Cases: ftle (fused C-G eigen/FTLE stencil, 4001 x 4001 flow map),
+    ridge (percentile + ridge points on that FTLE field), compose (72 maps of
+    the 676 x 251 grid), label (8-connected labelling of a 4001 x 4001 ridge
+    mask), batch (16 geophysical fields at 0.4 deg, tile schedule), mlp (one
+    BF16 gradient pass over 2^20 samples)."""
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300.extraction import ridges as R
+    n = 4001
+    lin = lambda a, b, k: torch.linspace(a, b, k, dtype=torch.float64, device="cuda")  # noqa: E731
+    X, Y = torch.meshgrid(lin(0, 2, n), lin(0, 1, n), indexing="ij")
+    fm = torch.stack([X + 0.1 * torch.sin(3 * Y) * torch.cos(2 * X),
+                      Y + 0.1 * torch.sin(2 * X) * torch.cos(3 * Y)], dim=-1).contiguous()
+    x, y = lin(0, 2, n), lin(0, 1, n)
+    dx, dy = 2.0 / (n - 1), 1.0 / (n - 1)
+    if name == "ftle":
+        fn = lambda: nb.ftle_evec_2D(fm, -10.0, dx, dy)  # noqa: E731
+    elif name == "ridge":
+        f, e = nb.ftle_evec_2D(fm, -10.0, dx, dy)
+        fn = lambda: nb.ftle_ridge_pts(f, e, x, y, 0.0, 90)  # noqa: E731
+    elif name == "label":
+        f, e = nb.ftle_evec_2D(fm, -10.0, dx, dy)
+        mask = R._ftle_ridges(f, e, x, y, 0.0, 50)[1]
+        fn = lambda: R.label8(mask)  # noqa: E731
+    elif name == "compose":
+        nx, ny, nT = 676, 251, 72
+        Xc, Yc = torch.meshgrid(lin(-100, 35, nx), lin(-5, 45, ny), indexing="ij")
+        fms = torch.stack([torch.stack([Xc + 0.3 * torch.sin(0.1 * Yc + k),
+                                        Yc + 0.3 * torch.cos(0.1 * Xc + k)], -1)
+                           for k in range(nT)]).contiguous()
+        fn = lambda: nb.flowmap_composition(fms, ((-100.0, 35.0, nx), (-5.0, 45.0, ny)), nT)  # noqa: E731
+    elif name == "batch":
+        from numbacs_gb300 import workloads as W
+        from numbacs_gb300.batch import Field, FTLEBatch
+        wl = geo_setup(180.0)
+        lonf, latf = W.geo_ftle_grid(0.4)
+        fields = [Field(wl["flow"], t0, T, lonf, latf, np.array([-1.0]), rtol=1e-7, atol=1e-9)
+                  for t0, T, _ in W.geo_batch_specs(seed=1)[:16]]
+        fn = FTLEBatch(fields, precision="mixed", blocks_per_sm=-1, graph=False).launch
+    else:
+        from numbacs_gb300.learned import StepProposer
+        g = torch.Generator(device="cuda").manual_seed(0)
+        feats = torch.randn((1 << 20, 8), generator=g, device="cuda")
+        targ = torch.randn((1 << 20,), generator=g, device="cuda")
+        sp = StepProposer(seed=0)
+        sp.set_normalization(feats, targ)
+        fn = lambda: sp.gradient(feats, targ)  # noqa: E731
+    fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    return {"kernel_case": name, "ms": times}
+
+
 def main():
     args = parse()
+    if args.kernel_case:
+        dist_setup()
+        print(json.dumps(run_kernel_case(args.kernel_case)))
+        return 0
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:

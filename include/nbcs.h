@@ -287,8 +287,9 @@ int nbcs_mlp_grad(const void* blob, const float* feats, const float* targets, in
 int nbcs_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1,
                   float beta2, float eps, int32_t step, void* blob, void* stream);
 /* Training data: integrate the grid with the mixed-precision plain
- * controller and, for a sampled fraction of step attempts (a hash of particle
- * and step, `sample` in [0, 1]), write the features at the step start to
+ * controller and, for a sampled fraction of the accepted steps that start
+ * and end inside the velocity grid (a hash of particle and step, `sample` in
+ * [0, 1]), write the features at the step start to
  * feats (capacity, 8) and the step that would have met the error target,
  * log(|h| * 0.9 * err^(-1/8)), to targets; *count (device uint64, caller
  * zeroes it) counts the samples offered, including any beyond capacity.

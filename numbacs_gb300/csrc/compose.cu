@@ -12,23 +12,23 @@
 // Interpolation is the interpolation package's eval_linear on a UCGrid with
 // extrapolation CONSTANT: 0 strictly outside the grid box (pinned by the
 // reference's composition fixtures: wall points that a map leaves 1 ulp
-// outside [0, 2] compose to 0).
+// outside [0, 2] compose to 0).  Arithmetic: cell offsets from the host-side
+// inverse spacing (n - 1) / (b - a) (GB300's FP64 pipe is narrow and a divide
+// is a multi-instruction sequence) and three explicit-FMA lerps per component,
+// the same operations as the oracle.
 #include "nbcs_internal.cuh"
 
 namespace nbcs {
 
 struct UGrid2 {
-    double x0, x1, y0, y1;
+    double x0, x1, y0, y1, dinvx, dinvy;  // dinv = (n - 1) / (b - a)
     int nx, ny;
 };
 
 // cell and offset of a point inside [a, b] on the uniform axis (a, b, n)
-__device__ __forceinline__ int lin_locate(double a, double b, int n, double x, double* lam)
+__device__ __forceinline__ int lin_locate(double a, double dinv, int n, double x, double* lam)
 {
-    if (x < a) x = a;
-    if (x > b) x = b;
-    double d = (b - a) / (double)(n - 1);
-    double u = (x - a) / d;
+    double u = (x - a) * dinv;
     int i = (int)floor(u);
     if (i > n - 2) i = n - 2;
     if (i < 0) i = 0;
@@ -42,14 +42,16 @@ __device__ __forceinline__ double2 bilinear2(const double2* __restrict__ f, cons
     if (px < g.x0 || px > g.x1 || py < g.y0 || py > g.y1) return make_double2(0.0, 0.0);
     if (px != px || py != py) return make_double2(px + py, px + py);  // NaN in, NaN out
     double l0, l1;
-    const int i = lin_locate(g.x0, g.x1, g.nx, px, &l0);
-    const int j = lin_locate(g.y0, g.y1, g.ny, py, &l1);
+    const int i = lin_locate(g.x0, g.dinvx, g.nx, px, &l0);
+    const int j = lin_locate(g.y0, g.dinvy, g.ny, py, &l1);
     const double2* r0 = f + (long)i * g.ny + j;
     const double2* r1 = r0 + g.ny;
     const double2 f00 = __ldg(r0), f01 = __ldg(r0 + 1), f10 = __ldg(r1), f11 = __ldg(r1 + 1);
     double2 v;
-    v.x = (1.0 - l0) * ((1.0 - l1) * f00.x + l1 * f01.x) + l0 * ((1.0 - l1) * f10.x + l1 * f11.x);
-    v.y = (1.0 - l0) * ((1.0 - l1) * f00.y + l1 * f01.y) + l0 * ((1.0 - l1) * f10.y + l1 * f11.y);
+    const double ax = __fma_rn(l1, f01.x - f00.x, f00.x), bx = __fma_rn(l1, f11.x - f10.x, f10.x);
+    const double ay = __fma_rn(l1, f01.y - f00.y, f00.y), by = __fma_rn(l1, f11.y - f10.y, f10.y);
+    v.x = __fma_rn(l0, bx - ax, ax);
+    v.y = __fma_rn(l0, by - ay, ay);
     return v;
 }
 
@@ -82,7 +84,8 @@ extern "C" int nbcs_flowmap_compose(const double* flowmaps, int32_t nT, int32_t 
         return set_error(NBCS_ERR_INVALID, "compose: grid needs b > a on both axes");
     if (nT < 1 || first < 0 || first >= nT)
         return set_error(NBCS_ERR_INVALID, "compose: need nT >= 1 and 0 <= first < nT");
-    const UGrid2 g = {grid[0], grid[1], grid[3], grid[4], (int)gnx, (int)gny};
+    const UGrid2 g = {grid[0], grid[1], grid[3], grid[4], (gnx - 1.0) / (grid[1] - grid[0]),
+                      (gny - 1.0) / (grid[4] - grid[3]), (int)gnx, (int)gny};
     const long m = (long)g.nx * g.ny;
     if (m > (1L << 40)) return set_error(NBCS_ERR_INVALID, "compose: grid too large");
     if (!flowmaps || !out ||

@@ -346,8 +346,9 @@ struct FlowSpline32 {
     // RHS plus its spatial Jacobian J = d(dy)/d(x, y) (row-major 2x2), from
     // the derivative of the B-spline basis; the metric factor 1/cos(lat) of
     // the spherical modes is held fixed (its own derivative is left out).
-    // Used for the learned step proposer's features.
-    __device__ __forceinline__ void eval_grad(float th, float ts, const float* yh, const float* ys,
+    // Used for the learned step proposer's features.  Returns false (and zero
+    // velocity and Jacobian) outside the grid box.
+    __device__ __forceinline__ bool eval_grad(float th, float ts, const float* yh, const float* ys,
                                               float* dy, float* J, const ParamsF& P) const
     {
         const float p0 = P.v[0];
@@ -365,7 +366,7 @@ struct FlowSpline32 {
         if (out) {
             dy[0] = dy[1] = 0.0f;
             J[0] = J[1] = J[2] = J[3] = 0.0f;
-            return;
+            return false;
         }
         bspline_w32(fx, wx);
         bspline_w32(fy, wy);
@@ -385,6 +386,7 @@ struct FlowSpline32 {
         J[1] = kx * r[3] * gy;  // du/dy
         J[2] = ky * r[4] * gx;  // dv/dx
         J[3] = ky * r[5] * gy;  // dv/dy
+        return true;
     }
 };
 

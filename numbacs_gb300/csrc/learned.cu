@@ -1,9 +1,9 @@
 // DOP853 with a learned step-size proposer (mixed precision, spline flows).
 //
 // Two uses of one warp-synchronous solver:
-//   LOG      -- the plain dop853 controller runs; a hashed fraction of step
-//               attempts writes (features at the step start, ideal log step)
-//               as training data;
+//   LOG      -- the plain dop853 controller runs; a hashed fraction of the
+//               accepted steps writes (features at the step start, ideal log
+//               step) as training data;
 //   PROPOSE  -- at every fresh step start the MLP of mlp.cuh proposes the
 //               step from the local features and that proposal meets the
 //               controller's (nbcs_opts.step_model_mode).  The embedded error
@@ -47,12 +47,15 @@ __device__ __forceinline__ unsigned hash32(unsigned a, unsigned b)
     return h;
 }
 
+// Features and stage-0 derivative at the step start; false when the particle
+// is outside the velocity grid (zero velocity: no proposal, no training sample,
+// the plain controller lets its steps grow to the end of the span).
 template <class Flow>
-__device__ __forceinline__ void step_features(const Flow& fl, F2 x, const F2* y, const ParamsF& P,
+__device__ __forceinline__ bool step_features(const Flow& fl, F2 x, const F2* y, const ParamsF& P,
                                               float* k0, float* f)
 {
     float yh[2] = {y[0].hi, y[1].hi}, ys[2] = {y[0].lo, y[1].lo}, J[4];
-    fl.eval_grad(x.hi, x.lo, yh, ys, k0, J, P);
+    const bool inside = fl.eval_grad(x.hi, x.lo, yh, ys, k0, J, P);
     const float p0 = P.v[0];
     f[0] = yh[0] + ys[0];
     f[1] = yh[1] + ys[1];
@@ -62,6 +65,7 @@ __device__ __forceinline__ void step_features(const Flow& fl, F2 x, const F2* y,
     f[5] = p0 * J[0];
     f[6] = p0 * J[1];
     f[7] = p0 * J[2];
+    return inside;
 }
 
 template <class Flow, bool LOG, bool PROPOSE>
@@ -77,7 +81,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
     const float posneg = span >= 0.f ? 1.f : -1.f;
     const float hmax = fabsf(span);
     int status = NBCS_PARTICLE_OK, nstep = 0;
-    bool last = false, reject = false, fresh = false;
+    bool last = false, reject = false, fresh = false, feat_ok = false;
     float feat[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float h = 0.f, yh[2], ys[2], kk[2];
     *acc = *rej = *nfcn = 0;
@@ -85,7 +89,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
 
     if (active) {  // HINIT, with f0 from the feature evaluation
         float f0[2];
-        step_features(fl, x, y, P, f0, feat);
+        feat_ok = step_features(fl, x, y, P, f0, feat);
         kc[0] = make_float2(f0[0], f0[1]);
         float dnf = 0.f, dny = 0.f;
 #pragma unroll
@@ -116,7 +120,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
         float h1 = der12 <= 1.0e-15f ? fmaxf(1.0e-6f, fabsf(h) * 1.0e-3f) : nbcs_root8f(0.01f / der12);
         h = copysignf(fminf(100.0f * fabsf(h), fminf(h1, hmax)), posneg);
         *nfcn += 2;
-        fresh = true;
+        fresh = feat_ok;
     }
 
     while (__any_sync(FULL, active)) {
@@ -201,17 +205,6 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             continue;
         }
         const float fac11 = nbcs_root8f(err);
-        if (LOG && lead && !last) {  // the clipped last step says nothing about the ideal step
-            const unsigned hv = hash32(pid ^ sink.seed, (unsigned)nstep);
-            if ((float)(hv >> 8) * (1.0f / 16777216.0f) < sink.sample) {
-                unsigned long long k = atomicAdd(sink.count, 1ull);
-                if ((long long)k < sink.capacity) {
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) sink.feats[k * 8 + i] = feat[i];
-                    sink.targets[k] = __logf(fabsf(h) * safe / fmaxf(fac11, 1.0e-3f));
-                }
-            }
-        }
         const float fac = fmaxf(facc2, fminf(facc1, fac11 / safe));
         float hnew = h / fac;
         if (err <= 1.0f) {
@@ -220,14 +213,32 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             x = f2_add(x, h, 0.f);
             y[0] = ynew[0];
             y[1] = ynew[1];
-            if (last) {
+            if (last) {  // the clipped last step says nothing about the ideal step
                 active = false;
                 continue;
             }
-            float k0[2];
-            step_features(fl, x, y, P, k0, feat);  // next step's stage 0
+            float k0[2], fnext[8];
+            const bool ok_next = step_features(fl, x, y, P, k0, fnext);  // next step's stage 0
+            // Training samples: accepted steps that start and end inside the
+            // velocity grid (a step across its edge meets the jump to zero
+            // velocity, and its tiny "ideal" step would teach the network to
+            // shorten steps everywhere).
+            if (LOG && lead && feat_ok && ok_next) {
+                const unsigned hv = hash32(pid ^ sink.seed, (unsigned)nstep);
+                if ((float)(hv >> 8) * (1.0f / 16777216.0f) < sink.sample) {
+                    unsigned long long k = atomicAdd(sink.count, 1ull);
+                    if ((long long)k < sink.capacity) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) sink.feats[k * 8 + i] = feat[i];
+                        sink.targets[k] = __logf(fabsf(h) * safe / fmaxf(fac11, 1.0e-3f));
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) feat[i] = fnext[i];
+            feat_ok = ok_next;
             kc[0] = make_float2(k0[0], k0[1]);
-            fresh = true;
+            fresh = feat_ok;
             if (fabsf(hnew) > hmax) hnew = posneg * hmax;
             if (reject) hnew = posneg * fminf(fabsf(hnew), fabsf(h));
             reject = false;

@@ -49,10 +49,18 @@ struct SelScratch {
     SelState st;
 };
 
-__device__ __forceinline__ unsigned long long dkey(double d)
+// order-preserving unsigned key of a double's bit pattern
+__device__ __forceinline__ unsigned long long dkey(unsigned long long u)
 {
-    unsigned long long u = (unsigned long long)__double_as_longlong(d);
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// NaN / +-inf tests on the bit pattern: the same answers as isnan() and
+// == +-INFINITY without FP64 compares, which issue on GB300's narrow FP64 pipe
+// (the selection passes are otherwise integer work)
+__device__ __forceinline__ bool bits_nan(unsigned long long u)
+{
+    return (u & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
 }
 
 __device__ __forceinline__ double dkey_decode(unsigned long long k)
@@ -92,13 +100,13 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
     unsigned int nn = 0, np = 0, nm = 0;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long)gridDim.x * blockDim.x) {
-        double v = f[i];
-        if (isnan(v)) { ++nn; continue; }
+        const unsigned long long u = (unsigned long long)__double_as_longlong(f[i]);
+        if (bits_nan(u)) { ++nn; continue; }
         if (first) {
-            if (v == INFINITY) ++np;
-            else if (v == -INFINITY) ++nm;
+            if (u == 0x7ff0000000000000ull) ++np;
+            else if (u == 0xfff0000000000000ull) ++nm;
         }
-        unsigned long long key = dkey(v);
+        const unsigned long long key = dkey(u);
         if ((key & pmask) != prefix) continue;
         atomicAdd(&h[(unsigned)(key >> shift) & dmask], 1u);
     }
@@ -168,9 +176,9 @@ sel_final_kernel(const double* __restrict__ f, long n, SelScratch* s, int mode, 
     unsigned long long mn = ~0ull;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long)gridDim.x * blockDim.x) {
-        double v = f[i];
-        if (isnan(v)) continue;
-        unsigned long long key = dkey(v);
+        const unsigned long long u = (unsigned long long)__double_as_longlong(f[i]);
+        if (bits_nan(u)) continue;
+        const unsigned long long key = dkey(u);
         if (key > kk && key < mn) mn = key;
     }
     for (int o = 16; o > 0; o >>= 1) {

@@ -29,8 +29,9 @@ def log_steps(flow, t0, T, x, y, params, rtol=1e-6, atol=1e-8, sample=1.0, seed=
               capacity=1 << 22):
     """Integrate the grid with the plain controller (mixed precision) and
     return (features (n, 8), targets (n,)) float32 CUDA tensors for a hashed
-    fraction ``sample`` of the step attempts (at most ``capacity`` rows) and
-    the number of samples offered."""
+    fraction ``sample`` of the accepted steps that start and end inside the
+    velocity grid (at most ``capacity`` rows) and the number of samples
+    offered."""
     D.require_cuda()
     flow = _check_callable_flow(flow)
     xd, yd = D.to_dev(x), D.to_dev(y)

@@ -755,15 +755,12 @@ void orc_c_eig_aux_2d(const double* F, int nx, int ny, double dx, double dy, dou
 
 /* --------------------------------------------------- flow-map composition */
 
-/* Cell and offset of x on the uniform axis (a, b, n) for multilinear
- * interpolation of a point inside [a, b]. */
-static int lin_locate(double a, double b, int n, double x, double* lam)
+/* Cell and offset of x on the uniform axis (a, n; dinv = (n-1)/(b-a)) for
+ * multilinear interpolation of a point inside [a, b]. */
+static int lin_locate(double a, double dinv, int n, double x, double* lam)
 {
     if (x != x) { *lam = x; return 0; }
-    if (x < a) x = a;
-    if (x > b) x = b;
-    double d = (b - a) / (double)(n - 1);
-    double u = (x - a) / d;
+    double u = (x - a) * dinv;
     int i = (int)floor(u);
     if (i > n - 2) i = n - 2;
     if (i < 0) i = 0;
@@ -780,13 +777,16 @@ static void bilinear2(const double* f, const double* g, int nx, int ny, double p
         return;
     }
     double l0, l1;
-    int i = lin_locate(g[0], g[1], nx, px, &l0);
-    int j = lin_locate(g[3], g[4], ny, py, &l1);
+    int i = lin_locate(g[0], ((double)nx - 1.0) / (g[1] - g[0]), nx, px, &l0);
+    int j = lin_locate(g[3], ((double)ny - 1.0) / (g[4] - g[3]), ny, py, &l1);
     const double* f00 = f + 2 * ((size_t)i * ny + j);
     const double* f10 = f00 + 2 * (size_t)ny;
-    for (int c = 0; c < 2; ++c)
-        r[c] = (1.0 - l0) * ((1.0 - l1) * f00[c] + l1 * f00[2 + c])
-             + l0 * ((1.0 - l1) * f10[c] + l1 * f10[2 + c]);
+    /* lerp along y in both rows, then along x (explicit FMAs) */
+    for (int c = 0; c < 2; ++c) {
+        double a = fma(l1, f00[2 + c] - f00[c], f00[c]);
+        double b = fma(l1, f10[2 + c] - f10[c], f10[c]);
+        r[c] = fma(l0, b - a, a);
+    }
 }
 
 /* integration.py:609-641 (flowmap_composition): the points start at the
