@@ -250,6 +250,16 @@ int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int
                    uint8_t* mask_out, double* rpts_full, double* pts_out, int64_t* n_out,
                    void* scratch, size_t scratch_bytes, void* stream);
 
+/* nbcs_ridge_pts with the threshold f_min and the grid spacing dx, dy given
+ * instead of a percentile of f and x[1] - x[0], y[1] - y[0] (no reference
+ * counterpart: a row block of a field sharded over several GPUs takes the
+ * global field's percentile, reduced on the host, and the global spacing).
+ * Same arguments and scratch otherwise. */
+int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, const double* x, int32_t nx,
+                        const double* y, int32_t ny, double dx, double dy, double sdd_thresh,
+                        double f_min, uint8_t* mask_out, double* rpts_full, double* pts_out,
+                        int64_t* n_out, void* scratch, size_t scratch_bytes, void* stream);
+
 /* 8-connected component labels of a mask (nx, ny) u8 -> labels (nx, ny)
  * int32: 0 background, 1..n numbered by each component's first pixel in
  * row-major order, exactly as scipy.ndimage.label with a 3x3 structure

@@ -76,6 +76,8 @@ SIGNATURES = {
     "nbcs_ftle_evec_2d": (ctypes.c_int, [_vp, _i32, _i32, _d, _d, _d, _vp, _vp, _vp, _vp]),
     "nbcs_percentile_scratch_bytes": (_sz, [_i64]),
     "nbcs_percentile": (ctypes.c_int, [_vp, _i64, _d, _vp, _vp, _sz, _vp]),
+    "nbcs_ridge_pts_fmin": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _d, _d, _vp,
+                                           _vp, _vp, _vp, _vp, _sz, _vp]),
     "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
                                       _vp, _sz, _vp]),

@@ -284,7 +284,14 @@ struct RidgeIn {
     double sdd;
     const double* fmin_ptr;  // device threshold (percentile) or NULL
     double fmin_val;         // threshold when fmin_ptr is NULL
+    double dx, dy;           // grid spacing; NaN: x[1] - x[0], y[1] - y[0] (ridges.py:39-40)
 };
+
+__device__ __forceinline__ void ridge_spacing(const RidgeIn& R, double* dx, double* dy)
+{
+    *dx = R.dx == R.dx ? R.dx : R.x[1] - R.x[0];
+    *dy = R.dy == R.dy ? R.dy : R.y[1] - R.y[0];
+}
 
 // Ridge test at point k = i*ny + j (ridges.py:52-74).  Returns true and the
 // sub-pixel point when (i, j) is a ridge point.
@@ -321,7 +328,8 @@ ridge_flag_kernel(RidgeIn R, uint8_t* __restrict__ mask, double2* __restrict__ r
                   unsigned int* __restrict__ block_count)
 {
     const long n = (long)R.nx * R.ny;
-    const double dx = R.x[1] - R.x[0], dy = R.y[1] - R.y[0];
+    double dx, dy;
+    ridge_spacing(R, &dx, &dy);
     const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
     const long base = (long)blockIdx.x * kRidgeTile;
     unsigned int c = 0;
@@ -378,7 +386,8 @@ ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
 {
     __shared__ unsigned int wsum[kRidgeThreads / 32];
     const long n = (long)R.nx * R.ny;
-    const double dx = R.x[1] - R.x[0], dy = R.y[1] - R.y[0];
+    double dx, dy;
+    ridge_spacing(R, &dx, &dy);
     const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
     const long base = (long)blockIdx.x * kRidgeTile;
     unsigned long long run = off[blockIdx.x];
@@ -443,10 +452,13 @@ extern "C" size_t nbcs_ridge_scratch_bytes(int32_t nx, int32_t ny)
            align256(sizeof(unsigned long long) * (size_t)nb) + align256((size_t)nx * ny);
 }
 
-extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int32_t nx,
-                              const double* y, int32_t ny, double sdd_thresh, double percentile,
-                              uint8_t* mask_out, double* rpts_full, double* pts_out,
-                              int64_t* n_out, void* scratch, size_t scratch_bytes, void* stream)
+// Ridge flags, points and compaction with the threshold f_min either taken
+// from the percentile selection (use_percentile, percentile != 0) or given.
+static int ridge_run(const double* f, const double* evec_max, const double* x, int32_t nx,
+                     const double* y, int32_t ny, double dx, double dy, double sdd_thresh,
+                     bool use_percentile, double percentile, double f_min, uint8_t* mask_out,
+                     double* rpts_full, double* pts_out, int64_t* n_out, void* scratch,
+                     size_t scratch_bytes, void* stream)
 {
     if (nx < 2 || ny < 2) return set_error(NBCS_ERR_INVALID, "ridge_pts: need nx, ny >= 2");
     if (!f || !evec_max || !x || !y || !pts_out || !n_out)
@@ -454,7 +466,7 @@ extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const dou
     if ((reinterpret_cast<uintptr_t>(evec_max) | reinterpret_cast<uintptr_t>(pts_out) |
          reinterpret_cast<uintptr_t>(rpts_full)) & 15)
         return set_error(NBCS_ERR_INVALID, "ridge_pts: evec/pts arrays must be 16-byte aligned");
-    if (!(percentile >= 0.0 && percentile <= 100.0))
+    if (use_percentile && !(percentile >= 0.0 && percentile <= 100.0))
         return set_error(NBCS_ERR_INVALID, "ridge_pts: percentile outside [0, 100]");
     size_t need = nbcs_ridge_scratch_bytes(nx, ny);
     if (!scratch || scratch_bytes < need)
@@ -478,9 +490,11 @@ extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const dou
     R.nx = nx;
     R.ny = ny;
     R.sdd = sdd_thresh;
+    R.dx = dx;
+    R.dy = dy;
     R.fmin_ptr = nullptr;
-    R.fmin_val = 0.0;
-    if (percentile != 0.0) {  // ridges.py:48-51
+    R.fmin_val = use_percentile ? 0.0 : f_min;
+    if (use_percentile && percentile != 0.0) {  // ridges.py:48-51
         int rc = percentile_enqueue(f, n, percentile, nullptr, sel, st);
         if (rc) return rc;
         R.fmin_ptr = &sel->st.result;
@@ -494,6 +508,27 @@ extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const dou
         R, mask, off, reinterpret_cast<double2*>(pts_out));
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
+}
+
+extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const double* x, int32_t nx,
+                              const double* y, int32_t ny, double sdd_thresh, double percentile,
+                              uint8_t* mask_out, double* rpts_full, double* pts_out,
+                              int64_t* n_out, void* scratch, size_t scratch_bytes, void* stream)
+{
+    return ridge_run(f, evec_max, x, nx, y, ny, NAN, NAN, sdd_thresh, true, percentile, 0.0,
+                     mask_out, rpts_full, pts_out, n_out, scratch, scratch_bytes, stream);
+}
+
+extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, const double* x,
+                                   int32_t nx, const double* y, int32_t ny, double dx, double dy,
+                                   double sdd_thresh, double f_min, uint8_t* mask_out,
+                                   double* rpts_full, double* pts_out, int64_t* n_out,
+                                   void* scratch, size_t scratch_bytes, void* stream)
+{
+    if (!(dx > 0.0 || dx < 0.0) || !(dy > 0.0 || dy < 0.0))
+        return set_error(NBCS_ERR_INVALID, "ridge_pts_fmin: dx, dy must be nonzero");
+    return ridge_run(f, evec_max, x, nx, y, ny, dx, dy, sdd_thresh, false, 0.0, f_min, mask_out,
+                     rpts_full, pts_out, n_out, scratch, scratch_bytes, stream);
 }
 
 // ---------------------------------------------------------------------------

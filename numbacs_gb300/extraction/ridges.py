@@ -13,7 +13,8 @@ from .. import _device as D
 from .. import _lib
 
 
-def _run(f, eigvec_max, x, y, sdd_thresh, percentile, want_mask, want_full):
+def _run(f, eigvec_max, x, y, sdd_thresh, percentile, want_mask, want_full, f_min=None,
+         dxdy=None):
     D.require_cuda()
     fd = D.to_dev(f)
     ev = D.to_dev(eigvec_max)
@@ -30,10 +31,41 @@ def _run(f, eigvec_max, x, y, sdd_thresh, percentile, want_mask, want_full):
     full = D.empty((nx * ny, 2)) if want_full else None
     pts = D.empty((nx * ny, 2))
     n_out = D.empty((1,), torch.int64)
-    _lib.check(L.nbcs_ridge_pts(D.ptr(fd), D.ptr(ev), D.ptr(xd), nx, D.ptr(yd), ny,
-                                float(sdd_thresh), float(percentile), D.ptr(mask), D.ptr(full),
-                                D.ptr(pts), D.ptr(n_out), D.ptr(scratch), nbytes, D.stream_ptr()))
+    if f_min is None:
+        _lib.check(L.nbcs_ridge_pts(D.ptr(fd), D.ptr(ev), D.ptr(xd), nx, D.ptr(yd), ny,
+                                    float(sdd_thresh), float(percentile), D.ptr(mask),
+                                    D.ptr(full), D.ptr(pts), D.ptr(n_out), D.ptr(scratch), nbytes,
+                                    D.stream_ptr()))
+    else:
+        _lib.check(L.nbcs_ridge_pts_fmin(D.ptr(fd), D.ptr(ev), D.ptr(xd), nx, D.ptr(yd), ny,
+                                         float(dxdy[0]), float(dxdy[1]), float(sdd_thresh),
+                                         float(f_min), D.ptr(mask),
+                                         D.ptr(full), D.ptr(pts), D.ptr(n_out), D.ptr(scratch),
+                                         nbytes, D.stream_ptr()))
     return pts, n_out, mask, full
+
+
+def ridge_pts_fmin(f, eigvec_max, x, y, dx, dy, sdd_thresh, f_min):
+    """ftle_ridge_pts with the threshold f_min and the spacing dx, dy given (a
+    row block of a field sharded over several GPUs: the global threshold and
+    spacing) -> ridge points (k, 2), row-major."""
+    as_torch = D.is_torch(f, eigvec_max)
+    pts, n_out, _, _ = _run(f, eigvec_max, x, y, sdd_thresh, 0, False, False, f_min=f_min,
+                            dxdy=(dx, dy))
+    return D.finish(pts[:int(n_out.item())], as_torch)
+
+
+def percentile(f, q):
+    """np.percentile(f, q) as the reference's numba code evaluates it (float)."""
+    D.require_cuda()
+    fd = D.to_dev(f).reshape(-1)
+    L = _lib.load()
+    nbytes = L.nbcs_percentile_scratch_bytes(fd.numel())
+    scratch = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=fd.device)
+    out = D.empty((1,))
+    _lib.check(L.nbcs_percentile(D.ptr(fd), fd.numel(), float(q), D.ptr(out), D.ptr(scratch),
+                                 nbytes, D.stream_ptr()))
+    return float(out.item())
 
 
 def ftle_ridge_pts(f, eigvec_max, x, y, sdd_thresh=0.0, percentile=0):

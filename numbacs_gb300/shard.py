@@ -1,0 +1,121 @@
+"""One FTLE field sharded over several GPUs: row blocks with halos.
+
+The particles of flowmap_grid_2D are independent, so a field splits into
+contiguous blocks of x rows, one per rank, with no exchange on the data path.
+The stencils that follow need neighbours: the FTLE at row i reads the flow map
+at rows i +- 1 and the ridge test at row i reads the FTLE at rows i +- 1, so a
+rank integrates its block plus HALO = 2 rows on each side (redundantly with
+its neighbours) and then owns exact FTLE values and ridge points for its own
+rows.  The one global quantity is the ridge threshold, np.percentile of the
+whole FTLE field (ridges.py:48-51): the owned FTLE rows (8 bytes per point)
+are gathered once over the process group, every rank computes the same exact
+percentile, and each extracts its rows' ridge points; gathering those in rank
+order gives the single-GPU result bit for bit (row-major order is preserved
+because the blocks are contiguous and in rank order).
+
+The compute goes through an ``ops`` object (flow map, FTLE + eigvec_max,
+percentile, thresholded ridge points): :class:`GpuOps` is the product path;
+a CPU object with the same methods lets the multi-process logic run as gloo
+ranks without GPUs.  Labelled ridges (``ftle_ridges``) are not sharded: a
+component crossing a block boundary needs a merge step that is not built.
+"""
+import numpy as np
+
+HALO = 2
+
+
+def row_blocks(nx, world):
+    """Owned rows [i0, i1) of each rank: contiguous, in rank order, sizes
+    differing by at most one."""
+    if world < 1 or nx < world:
+        raise ValueError("need 1 <= world <= nx")
+    base, extra = divmod(nx, world)
+    blocks, i0 = [], 0
+    for r in range(world):
+        i1 = i0 + base + (1 if r < extra else 0)
+        blocks.append((i0, i1))
+        i0 = i1
+    return blocks
+
+
+def extended_rows(i0, i1, nx, halo=HALO):
+    """Rows a rank integrates: its block plus `halo` rows each side, clipped."""
+    return max(0, i0 - halo), min(nx, i1 + halo)
+
+
+class GpuOps:
+    """The product path: the CUDA library through the drop-in functions."""
+
+    def flowmap(self, flow, t0, T, x, y, params, **kw):
+        from .integration import flowmap_grid_2D
+        return flowmap_grid_2D(flow, t0, T, x, y, params, **kw)
+
+    def ftle_evec(self, fm, T, dx, dy):
+        from .diagnostics import ftle_evec_2D
+        return ftle_evec_2D(fm, T, dx, dy)
+
+    def percentile(self, f, q):
+        from .extraction.ridges import percentile
+        return percentile(f, q)
+
+    def ridge_pts(self, f, evec, x, y, dx, dy, sdd_thresh, f_min):
+        from .extraction.ridges import ridge_pts_fmin
+        return ridge_pts_fmin(f, evec, x, y, dx, dy, sdd_thresh, f_min)
+
+    def to_numpy(self, a):
+        return a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
+
+
+def block_ftle(ops, rank, world, flow, t0, T, x, y, params, **flowmap_kw):
+    """Phase 1 on one rank: flow map, FTLE and eigvec_max of the rank's
+    extended block.  Returns (state, owned FTLE rows as numpy)."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    nx = len(x)
+    i0, i1 = row_blocks(nx, world)[rank]
+    e0, e1 = extended_rows(i0, i1, nx)
+    dx, dy = x[1] - x[0], y[1] - y[0]  # the global spacing (ridges.py:39-40)
+    fm = ops.flowmap(flow, t0, T, x[e0:e1], y, params, **flowmap_kw)
+    f, ev = ops.ftle_evec(fm, T, dx, dy)
+    state = {"f": f, "ev": ev, "x": x[e0:e1], "y": y, "d": (dx, dy), "rows": (i0, i1, e0, e1)}
+    return state, ops.to_numpy(f)[i0 - e0:i1 - e0]
+
+
+def block_ridge_pts(ops, state, f_global, sdd_thresh=0.0, percentile=0):
+    """Phase 2 on one rank: the global threshold from the whole FTLE field
+    (0 when percentile == 0, as ridges.py:48-51) and the ridge points of the
+    rank's rows (the extended block's 2-row border, which the stencil skips,
+    is exactly its halo)."""
+    f_min = 0.0 if percentile == 0 else ops.percentile(f_global, percentile)
+    dx, dy = state["d"]
+    pts = ops.ridge_pts(state["f"], state["ev"], state["x"], state["y"], dx, dy, sdd_thresh,
+                        f_min)
+    return ops.to_numpy(pts)
+
+
+def sharded_ftle_ridge_pts(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile=0, *,
+                           group=None, ops=None, **flowmap_kw):
+    """ftle_ridge_pts of the field's flow map, computed by every rank of the
+    process group on its row block; every rank returns the full (k, 2) numpy
+    array of ridge points, identical to the one-GPU pipeline
+    flowmap_grid_2D -> ftle_evec_2D -> ftle_ridge_pts.  Collectives: two
+    all_gather_object calls on the host (owned FTLE rows, ridge points)."""
+    import torch.distributed as dist
+    ops = ops or GpuOps()
+    if dist.is_available() and dist.is_initialized():
+        rank, world = dist.get_rank(group), dist.get_world_size(group)
+    else:
+        rank, world = 0, 1
+    state, owned = block_ftle(ops, rank, world, flow, t0, T, x, y, params, **flowmap_kw)
+    if world == 1:
+        rows = [owned]
+    else:
+        rows = [None] * world
+        dist.all_gather_object(rows, owned, group=group)
+    f_global = np.concatenate(rows, axis=0)
+    pts = block_ridge_pts(ops, state, f_global, sdd_thresh, percentile)
+    if world == 1:
+        return pts
+    parts = [None] * world
+    dist.all_gather_object(parts, pts, group=group)
+    return np.concatenate(parts, axis=0)

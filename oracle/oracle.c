@@ -612,12 +612,23 @@ double orc_percentile(const double* f, int64_t n, double q)
 
 /* extraction/ridges.py:79-154 (_ftle_ridges); ftle_ridge_pts (:9-76) is the
  * row-major compaction of rpts_full over mask_out. */
+void orc_ridge_field_d(const double* f, const double* ev, const double* x, int nx,
+                       const double* y, int ny, double dx, double dy, double sdd_thresh,
+                       double f_min, uint8_t* mask_out, double* rpts);
+
 void orc_ridge_field(const double* f, const double* ev, const double* x, int nx,
                      const double* y, int ny, double sdd_thresh, double f_min,
                      uint8_t* mask_out, double* rpts)
 {
-    double dx = x[1] - x[0];
-    double dy = y[1] - y[0];
+    orc_ridge_field_d(f, ev, x, nx, y, ny, x[1] - x[0], y[1] - y[0], sdd_thresh, f_min,
+                      mask_out, rpts);
+}
+
+/* the same with the grid spacing given (a row block of a sharded field) */
+void orc_ridge_field_d(const double* f, const double* ev, const double* x, int nx,
+                       const double* y, int ny, double dx, double dy, double sdd_thresh,
+                       double f_min, uint8_t* mask_out, double* rpts)
+{
     memset(mask_out, 0, (size_t)nx * ny);
     memset(rpts, 0, sizeof(double) * 2 * (size_t)nx * ny);
 #ifdef _OPENMP

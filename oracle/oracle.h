@@ -79,6 +79,9 @@ double orc_percentile(const double* f, int64_t n, double q);
 void orc_ridge_field(const double* f, const double* evec, const double* x, int nx,
                      const double* y, int ny, double sdd_thresh, double f_min,
                      uint8_t* mask_out, double* rpts_full);
+void orc_ridge_field_d(const double* f, const double* evec, const double* x, int nx,
+                       const double* y, int ny, double dx, double dy, double sdd_thresh,
+                       double f_min, uint8_t* mask_out, double* rpts_full);
 
 /* flowmap_aux_grid_2D: out (nx,ny,n_aux,2), n_aux = 5 (eig_main) or 4 */
 int orc_flowmap_aux_grid_2d(const orc_flow* flow, double t0, double T, const double* x, int nx,

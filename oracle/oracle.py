@@ -78,6 +78,7 @@ def lib():
         L.orc_percentile.argtypes = [vp, i64, d]
         L.orc_percentile.restype = d
         L.orc_ridge_field.argtypes = [vp, vp, vp, i, vp, i, d, d, vp, vp]
+        L.orc_ridge_field_d.argtypes = [vp, vp, vp, i, vp, i, d, d, d, d, vp, vp]
         L.orc_flowmap_aux_grid_2d.argtypes = [vp, d, d, vp, i, vp, i, vp, d, i, i, d, d, vp, vp,
                                               vp, vp, i, i]
         L.orc_c_eig_aux_2d.argtypes = [vp, i, i, d, d, d, i, vp, vp, vp]
@@ -280,22 +281,34 @@ def ridge_field(f, eigvec_max, x, y, sdd_thresh=0.0, percentile_=0):
     return _ridge_field(f, eigvec_max, x, y, sdd_thresh, percentile_)
 
 
-def _ridge_field(f, eigvec_max, x, y, sdd_thresh=0.0, percentile_=0):
+def _ridge_field(f, eigvec_max, x, y, sdd_thresh=0.0, percentile_=0, f_min=None, dxdy=None):
     f = np.ascontiguousarray(f, np.float64)
     ev = np.ascontiguousarray(eigvec_max, np.float64)
     x = np.ascontiguousarray(x, np.float64)
     y = np.ascontiguousarray(y, np.float64)
     nx, ny = f.shape
-    f_min = 0.0 if percentile_ == 0 else percentile(f, percentile_)
+    if f_min is None:
+        f_min = 0.0 if percentile_ == 0 else percentile(f, percentile_)
     mask = np.zeros((nx, ny), np.uint8)
     rpts = np.zeros((nx * ny, 2))
-    lib().orc_ridge_field(_dp(f), _dp(ev), _dp(x), nx, _dp(y), ny, float(sdd_thresh),
-                          float(f_min), _dp(mask), _dp(rpts))
+    if dxdy is None:
+        lib().orc_ridge_field(_dp(f), _dp(ev), _dp(x), nx, _dp(y), ny, float(sdd_thresh),
+                              float(f_min), _dp(mask), _dp(rpts))
+    else:
+        lib().orc_ridge_field_d(_dp(f), _dp(ev), _dp(x), nx, _dp(y), ny, float(dxdy[0]),
+                                float(dxdy[1]), float(sdd_thresh), float(f_min), _dp(mask),
+                                _dp(rpts))
     return rpts, mask.astype(bool), f_min
 
 
 def ftle_ridge_pts(f, eigvec_max, x, y, sdd_thresh=0.0, percentile=0):
     rpts, mask, _ = _ridge_field(f, eigvec_max, x, y, sdd_thresh, percentile)
+    return rpts[mask.ravel()]
+
+
+def ridge_pts_fmin(f, eigvec_max, x, y, dx, dy, sdd_thresh, f_min):
+    """ftle_ridge_pts with the threshold and the grid spacing given."""
+    rpts, mask, _ = _ridge_field(f, eigvec_max, x, y, sdd_thresh, f_min=f_min, dxdy=(dx, dy))
     return rpts[mask.ravel()]
 
 
