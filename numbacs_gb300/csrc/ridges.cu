@@ -293,6 +293,17 @@ __device__ __forceinline__ void ridge_spacing(const RidgeIn& R, double* dx, doub
     *dy = R.dy == R.dy ? R.dy : R.y[1] - R.y[0];
 }
 
+// a > b for doubles given as bit patterns, by integer comparison (IEEE
+// semantics: false when either is NaN, -0 == +0); the ridge threshold test runs
+// on every point and an FP64 compare would issue on the narrow FP64 pipe
+__device__ __forceinline__ bool gt_bits(unsigned long long a, unsigned long long b)
+{
+    if (bits_nan(a) || bits_nan(b)) return false;
+    if ((a << 1) == 0) a = 0;  // -0 -> +0
+    if ((b << 1) == 0) b = 0;
+    return dkey(a) > dkey(b);
+}
+
 // Ridge test at point k = i*ny + j (ridges.py:52-74).  Returns true and the
 // sub-pixel point when (i, j) is a ridge point.
 __device__ __forceinline__ bool ridge_at(const RidgeIn& R, double fmin, double dx, double dy, long k,
@@ -303,7 +314,9 @@ __device__ __forceinline__ bool ridge_at(const RidgeIn& R, double fmin, double d
     if (i < 2 || i >= R.nx - 2 || j < 2 || j >= ny - 2) return false;
     const double* f = R.f;
     double f0 = f[k];
-    if (!(f0 > fmin)) return false;
+    if (!gt_bits((unsigned long long)__double_as_longlong(f0),
+                 (unsigned long long)__double_as_longlong(fmin)))
+        return false;
     double fip = f[k + ny], fim = f[k - ny], fjp = f[k + 1], fjm = f[k - 1];
     double fx = (fip - fim) / (2.0 * dx);
     double fy = (fjp - fjm) / (2.0 * dy);

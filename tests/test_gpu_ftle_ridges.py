@@ -133,6 +133,29 @@ def test_ridge_mask_bit_identical(nb, orc, shape, pct, sdd):
     assert np.array_equal(pts, orc.ftle_ridge_pts(f, e, x, y, sdd, pct))
 
 
+@pytest.mark.parametrize("pct", [0, 60])
+def test_ridge_threshold_special_values(nb, orc, pct):
+    """The threshold test f > f_min on NaN, +-0, +-inf and values equal to the
+    threshold: masks and points bit-identical to the oracle (the kernel
+    compares bit patterns as integers)."""
+    nx, ny = 48, 40
+    x, y, fm = _ridge_field(nx, ny, seed=3)
+    dx, dy = x[1] - x[0], y[1] - y[0]
+    oev, ovec = orc.C_eig_2D(fm, dx, dy)
+    f = orc.ftle_from_eig(oev[..., 1], 5.0)
+    e = np.ascontiguousarray(ovec[..., :, 1])
+    rng = np.random.default_rng(7)
+    thr = 0.0 if pct == 0 else orc.percentile(f, pct)
+    for v in (np.nan, 0.0, -0.0, np.inf, -np.inf, thr, np.nextafter(thr, np.inf),
+              np.nextafter(thr, -np.inf)):
+        idx = rng.integers(2, nx - 2, 12), rng.integers(2, ny - 2, 12)
+        f[idx] = v
+    r_pts, rb, _, _ = nb.extraction._ftle_ridges(f, e, x, y, 0.0, pct)
+    orp, orb, _ = orc.ridge_field(f, e, x, y, 0.0, pct)
+    assert np.array_equal(rb, orb)
+    assert np.array_equal(r_pts, orp, equal_nan=True)
+
+
 def test_ridge_compaction_large(nb):
     # size-independent properties at a large size: count == mask sum, the
     # compacted list is the row-major gather of the full array
