@@ -84,7 +84,7 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
     opts.lanes_per_particle = int(lanes_per_particle)
     opts.blocks_per_sm = int(blocks_per_sm)
     if step_model is not None:
-        opts.step_model = step_model.blob.data_ptr()
+        opts.step_model = step_model.proposal_blob().data_ptr()
         opts.step_model_mode = int(step_model_mode)
     opts.stats = stats.data_ptr() if stats is not None else None
     L = _lib.load()

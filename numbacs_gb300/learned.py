@@ -74,6 +74,9 @@ class StepProposer:
         self.norm[8:16] = 1.0
         self.norm[17] = 1.0
         self.step = 0
+        self.margin = 0.0  # log of the proposal margin (see proposal_blob)
+        self._version = 0
+        self._proposal = None
         self._write_norm()
         self._pack()
 
@@ -81,9 +84,26 @@ class StepProposer:
     def _write_norm(self):
         hdr = self.blob[:72].view(torch.float32)
         hdr[:18] = torch.from_numpy(self.norm[:18]).to(D.device())
+        self._version += 1
 
     def _pack(self):
         _lib.check(_lib.load().nbcs_mlp_pack(D.ptr(self.params), D.ptr(self.blob), D.stream_ptr()))
+        self._version += 1
+
+    def proposal_blob(self):
+        """The blob the integrator proposes steps with: the trained network
+        with its log-step output shifted by ``margin``.  The network predicts
+        the ideal step with a log-space error of about one standard
+        deviation, and min(proposal, controller) picks that error's low tail;
+        a margin > 0 lets the proposal cut only steps it is confident are too
+        long.  ``margin`` is calibrated on training flows (bench.py)."""
+        key = (self._version, float(self.margin))
+        if self._proposal is None or self._proposal[0] != key:
+            b = self.blob.clone()
+            hdr = b[:72].view(torch.float32)
+            hdr[16] = float(self.norm[16]) + float(self.margin)
+            self._proposal = (key, b)
+        return self._proposal[1]
 
     def set_normalization(self, feats, targets):
         f = feats.double()
@@ -128,6 +148,7 @@ class StepProposer:
                                              ctypes.c_float(beta1), ctypes.c_float(beta2),
                                              ctypes.c_float(eps), self.step, D.ptr(self.blob),
                                              D.stream_ptr()))
+        self._version += 1
 
     def train(self, feats, targets, epochs=4, batch=65536, lr=3e-3, lr_final=3e-4, seed=0,
               val=None, log=None):
@@ -160,7 +181,8 @@ class StepProposer:
         return hist
 
     def save(self, path):
-        np.savez(path, params=self.params.cpu().numpy(), norm=self.norm, step=self.step)
+        np.savez(path, params=self.params.cpu().numpy(), norm=self.norm, step=self.step,
+                 margin=self.margin)
 
     @classmethod
     def load(cls, path):
@@ -169,6 +191,7 @@ class StepProposer:
         sp.params.copy_(torch.from_numpy(z["params"]).to(sp.params.device))
         sp.norm = z["norm"].astype(np.float32)
         sp.step = int(z["step"])
+        sp.margin = float(z["margin"]) if "margin" in z.files else 0.0
         sp._write_norm()
         sp._pack()
         return sp
