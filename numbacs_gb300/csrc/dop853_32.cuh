@@ -99,6 +99,42 @@ __device__ __forceinline__ float f2_minus(F2 a, F2 b)  // (a - b) rounded to flo
     return (a.hi - b.hi) + (a.lo - b.lo);
 }
 
+// Stage argument combination sum_{j<S} a_Sj k_j for a compile-time stage S:
+// exactly S terms, the tableau entries as constant-bank operands.
+template <int S>
+__device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* a1)
+{
+    float x = 0.f, y = 0.f;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+        const float2 kj = kc[j * kThreads32];
+        x = fmaf(kA32[S][j], kj.x, x);
+        y = fmaf(kA32[S][j], kj.y, y);
+    }
+    *a0 = x;
+    *a1 = y;
+}
+
+// The same for a runtime stage s that is uniform across the warp (one branch
+// of a jump table instead of eleven predicated terms per stage).
+__device__ __forceinline__ void stage_combo(int s, const float2* kc, float* a0, float* a1)
+{
+    switch (s) {
+    case 0: *a0 = 0.f; *a1 = 0.f; break;
+    case 1: stage_combo<1>(kc, a0, a1); break;
+    case 2: stage_combo<2>(kc, a0, a1); break;
+    case 3: stage_combo<3>(kc, a0, a1); break;
+    case 4: stage_combo<4>(kc, a0, a1); break;
+    case 5: stage_combo<5>(kc, a0, a1); break;
+    case 6: stage_combo<6>(kc, a0, a1); break;
+    case 7: stage_combo<7>(kc, a0, a1); break;
+    case 8: stage_combo<8>(kc, a0, a1); break;
+    case 9: stage_combo<9>(kc, a0, a1); break;
+    case 10: stage_combo<10>(kc, a0, a1); break;
+    default: stage_combo<11>(kc, a0, a1); break;
+    }
+}
+
 // Integrate one particle (y, as compensated pairs) over solver time [x, xend].
 // `kc` is this thread's shared-memory column of stage derivatives (stride
 // kThreads32).  Returns an NBCS_PARTICLE_* code.
@@ -169,18 +205,13 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
         nstep++;
         yh[0] = y[0].hi;
         yh[1] = y[1].hi;
+        // every lane counts the stages from 0 (a rejected step skips stage 0,
+        // whose derivative is still valid) so the stage index is warp-uniform
 #pragma unroll 1
-        for (int s = fsal ? 0 : 1; s < 12; ++s) {
-            float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-            for (int j = 0; j < 11; ++j) {
-                if (j < s) {
-                    const float c = kA32[s][j];
-                    const float2 kj = kc[j * kThreads32];
-                    a0 = fmaf(c, kj.x, a0);
-                    a1 = fmaf(c, kj.y, a1);
-                }
-            }
+        for (int s = 0; s < 12; ++s) {
+            if (s == 0 && !fsal) continue;
+            float a0, a1;
+            stage_combo(s, kc, &a0, &a1);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
             fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);

@@ -163,17 +163,18 @@ __device__ __forceinline__ void bspline_w32(float t, float* w)
     w[3] = s * t2 * t;
 }
 
-// B-spline weight of time level a in {0..3} at offset t (one basis function)
+// B-spline weight of time level a in {0..3} at offset t (one basis function),
+// branch-free: the lanes of a group take different levels, and a switch on a
+// lane-dependent index would serialise the cases.  6 w_a(t) = c3 t^3 + c2 t^2 +
+// c1 t + c0 with (c3, c2, c1, c0) = (-1, 3, -3, 1), (3, -6, 0, 4), (-3, 3, 3, 1),
+// (1, 0, 0, 0).
 __device__ __forceinline__ float bspline_w32_one(float t, int a)
 {
-    const float s = 1.0f / 6.0f;
-    float t2 = t * t, u = 1.0f - t;
-    switch (a) {
-    case 0: return s * u * u * u;
-    case 1: return s * fmaf(fmaf(3.0f, t, -6.0f), t2, 4.0f);
-    case 2: return s * fmaf(fmaf(fmaf(-3.0f, t, 3.0f), t, 3.0f), t, 1.0f);
-    default: return s * t2 * t;
-    }
+    const float c3 = a == 0 ? -1.0f : a == 1 ? 3.0f : a == 2 ? -3.0f : 1.0f;
+    const float c2 = a == 0 ? 3.0f : a == 1 ? -6.0f : a == 2 ? 3.0f : 0.0f;
+    const float c1 = a == 0 ? -3.0f : a == 2 ? 3.0f : 0.0f;
+    const float c0 = a == 0 ? 1.0f : a == 1 ? 4.0f : a == 2 ? 1.0f : 0.0f;
+    return (1.0f / 6.0f) * fmaf(fmaf(fmaf(c3, t, c2), t, c1), t, c0);
 }
 
 // Group-cooperative tricubic evaluation.  Coefficients use the "quad" layout:
@@ -335,7 +336,8 @@ struct FlowSpline32 {
         spline_eval_uv32<LP>(g, c, it, ix, iy, ft, wx, wy, &u, &v);
         if (SPH == 1 || SPH == 2) {
             float lat = yh[1] + ys[1];
-            dy[0] = p0 * u * deg_per_km / cospif(lat * (1.0f / 180.0f));
+            // approximate reciprocal (2 ulp): far inside the FP32 stage error
+            dy[0] = __fdividef(p0 * u * deg_per_km, cospif(lat * (1.0f / 180.0f)));
             dy[1] = p0 * v * deg_per_km;
         } else {
             dy[0] = p0 * u;

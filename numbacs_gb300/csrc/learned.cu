@@ -158,16 +158,8 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
         yh[1] = y[1].hi;
 #pragma unroll 1
         for (int s = 1; s < 12; ++s) {
-            float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-            for (int j = 0; j < 11; ++j) {
-                if (j < s) {
-                    const float c = kA32[s][j];
-                    const float2 kj = kc[j * kThreads32];
-                    a0 = fmaf(c, kj.x, a0);
-                    a1 = fmaf(c, kj.y, a1);
-                }
-            }
+            float a0, a1;
+            stage_combo(s, kc, &a0, &a1);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
             fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);
