@@ -19,6 +19,8 @@ imported here because numba / numbalsoda / interpolation are absent):
                                     (tests/test_integration.py:66-75)
   tests/testing_data/Cevals_aux.npy, C_eig_aux_2D(fm_aux, 0.1, 0.1)  (tests/test_diagnostics.py:112-131)
   tests/testing_data/Cevecs_aux.npy
+  tests/testing_data/ordered_ridges.pkl  ftle_ordered_ridges(ftle, Cevecs[...,1], x, y, 0.1)
+                                    (tests/test_extraction.py:22-28)
   tests/test_flows.py literals      spline coefficients Cu/Cv (:74-133), spline values at 27
                                     points (:208-229), double-gyre and Bickley velocities
                                     at the same 27 points (:315-357)
@@ -98,6 +100,10 @@ def main(ref_root):
     arrays["n_ridges"] = np.array(len(ridges))
     for k, r in enumerate(ridges):
         arrays["ridges_%d" % k] = np.asarray(r)
+    ordered = _load_pkl(os.path.join(td, "ordered_ridges.pkl"))
+    arrays["n_ordered"] = np.array(len(ordered))
+    for k, r in enumerate(ordered):
+        arrays["ordered_%d" % k] = np.asarray(r)
     lit = _test_literals(os.path.join(ref_root, "tests", "test_flows.py"))
     arrays["spline_Cu"] = lit[("test_get_interp_arrays_2D", "Cu_expected")]
     arrays["spline_Cv"] = lit[("test_get_interp_arrays_2D", "Cv_expected")]

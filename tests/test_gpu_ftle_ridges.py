@@ -217,3 +217,34 @@ def test_ridges_large_field_groups(nb):
 def orc_like_eig(fm, dx, dy):
     import oracle
     return oracle.C_eig_2D(fm, dx, dy)
+
+
+def test_ordered_ridges_golden(nb, golden, coords_dg):
+    """tests/test_extraction.py:22-28 through the drop-in (GPU ridge test)."""
+    x, y = coords_dg
+    f = golden["ftle"].astype(np.float64)
+    e = np.ascontiguousarray(golden["Cevecs"][:, :, :, 1].astype(np.float64))
+    ridges = nb.ftle_ordered_ridges(f, e, x, y, 0.1)
+    n = int(golden["n_ordered"])
+    assert len(ridges) == n
+    for k in range(n):
+        assert np.allclose(ridges[k], golden["ordered_%d" % k])
+
+
+@pytest.mark.parametrize("pct", [0, 80])
+def test_ordered_ridges_match_oracle_fed(nb, orc, pct):
+    """A larger field: the GPU-fed ordered ridges equal the oracle-fed ones
+    (same host linking, bit-identical ridge tests)."""
+    from numbacs_gb300.extraction.ordered import ordered_from_ridge_field
+    nx, ny = 301, 157
+    x, y, fm = _ridge_field(nx, ny, seed=5)
+    dx, dy = x[1] - x[0], y[1] - y[0]
+    oev, ovec = orc.C_eig_2D(fm, dx, dy)
+    f = orc.ftle_from_eig(oev[..., 1], 5.0)
+    e = np.ascontiguousarray(ovec[..., :, 1])
+    ridges = nb.ftle_ordered_ridges(f, e, x, y, 3 * dx, percentile=pct)
+    rpts, mask, _ = orc.ridge_field(f, e, x, y, 0.0, pct)
+    ref = ordered_from_ridge_field(f, e, x, y, mask, rpts, 3 * dx)
+    assert len(ridges) == len(ref) and len(ref) > 0
+    for a, b in zip(ridges, ref):
+        assert np.array_equal(a, b)

@@ -217,3 +217,37 @@ def test_C_eig_aux_2D(orc, golden, mask_dg):
     ev4, vec4 = orc.C_eig_aux_2D(fa[:, :, :4], 0.1, 0.1, eig_main=False)
     assert np.array_equal(vec4[2:-2, 2:-2], vec[2:-2, 2:-2])
     assert (ev4[1:-1, 1:-1, 1] > 0).all()
+
+
+def test_ordered_ridges_golden(orc, golden, coords_dg):
+    """tests/test_extraction.py:22-28: the host-side linking of
+    numbacs_gb300.extraction.ordered fed by the oracle's ridge test."""
+    from numbacs_gb300.extraction.ordered import ordered_from_ridge_field
+    x, y = coords_dg
+    f = golden["ftle"].astype(np.float64)
+    e = np.ascontiguousarray(golden["Cevecs"][:, :, :, 1].astype(np.float64))
+    rpts, mask, _ = orc.ridge_field(f, e, x, y)
+    ridges = ordered_from_ridge_field(f, e, x, y, mask, rpts, 0.1)
+    n = int(golden["n_ordered"])
+    assert len(ridges) == n
+    for k in range(n):
+        assert ridges[k].shape == golden["ordered_%d" % k].shape
+        assert np.allclose(ridges[k], golden["ordered_%d" % k])
+
+
+def test_ordered_ridges_options(orc, golden, coords_dg):
+    """min_ridge_pts and the endpoint tolerances act as filters: fewer or equal
+    curves, every curve one of the ridge points' paths."""
+    from numbacs_gb300.extraction.ordered import ordered_from_ridge_field
+    x, y = coords_dg
+    f = golden["ftle"].astype(np.float64)
+    e = np.ascontiguousarray(golden["Cevecs"][:, :, :, 1].astype(np.float64))
+    rpts, mask, _ = orc.ridge_field(f, e, x, y)
+    pts = {tuple(p) for p in rpts[mask.ravel()]}
+    for kw in ({"min_ridge_pts": 2}, {"min_ridge_pts": 7}, {"dist_tol": 1e-3},
+               {"ep_tan_ang": 0.1}):
+        args = dict(dist_tol=0.1)
+        args.update(kw)
+        ridges = ordered_from_ridge_field(f, e, x, y, mask, rpts, args.pop("dist_tol"), **args)
+        for r in ridges:
+            assert all(tuple(p) in pts for p in r)
