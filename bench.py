@@ -751,42 +751,76 @@ def run_rows(wl, rtol, nT=72):
 
 
 def run_e2e(nb, D, wl, prec, rtol, atol, args, world):
-    """Same step through the public numpy API: host arrays in, host results out."""
+    """The step through the public API, timed on the host clock: every step
+    copies its inputs (the particle grid) from pinned host memory to the GPU,
+    runs flow map -> FTLE/eigvec -> ridge points on device tensors and reads
+    the ridge points back into pinned host memory.  Reported beside it: the
+    numpy-everywhere use of the same calls (each call takes and returns
+    pageable numpy arrays, so the flow map and the FTLE field round-trip
+    through the host between calls)."""
     import torch
     lonf, latf = wl["lonf"], wl["latf"]
+    xh = torch.from_numpy(lonf).pin_memory()
+    yh = torch.from_numpy(latf).pin_memory()
+    out_h = torch.empty((len(lonf) * len(latf), 2), dtype=torch.float64).pin_memory()
+    moved = {"h2d": 0, "d2h": 0}
 
-    def step():
+    def step_pinned():
+        x = xh.to("cuda", non_blocking=True)
+        y = yh.to("cuda", non_blocking=True)
+        fm = nb.flowmap_grid_2D(wl["flow"], wl["t0"], wl["T"], x, y, wl["params"], rtol=rtol,
+                                atol=atol, precision=prec, return_status=True)[0]
+        f, e = nb.ftle_evec_2D(fm, wl["T"], wl["dx"], wl["dy"])
+        pts = nb.ftle_ridge_pts(f, e, x, y, 0.0, wl["pct"])
+        out_h[:pts.shape[0]].copy_(pts, non_blocking=True)
+        moved["h2d"] += xh.numel() * 8 + yh.numel() * 8
+        moved["d2h"] += pts.shape[0] * 16 + 8  # the points and their count
+        return pts.shape[0]
+
+    def step_numpy():
         fm = nb.flowmap_grid_2D(wl["flow"], wl["t0"], wl["T"], lonf, latf, wl["params"], rtol=rtol,
                                 atol=atol, precision=prec, return_status=True)[0]
         f, e = nb.ftle_evec_2D(fm, wl["T"], wl["dx"], wl["dy"])
         return nb.ftle_ridge_pts(f, e, lonf, latf, 0.0, wl["pct"])
 
-    for _ in range(2):
-        step()
-    torch.cuda.synchronize()
-    h0, d0 = D.transfer_bytes["h2d"], D.transfer_bytes["d2h"]
     K = max(3, args.steps)
-    barrier(world)
-    t = time.perf_counter()
-    for _ in range(K):
-        step()
-    torch.cuda.synchronize()
-    barrier(world)
-    dt = (time.perf_counter() - t) / K
-    dt = max_over_ranks(dt, world)
+
+    def timed(step):
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        barrier(world)
+        t = time.perf_counter()
+        for _ in range(K):
+            step()
+        torch.cuda.synchronize()
+        barrier(world)
+        return max_over_ranks((time.perf_counter() - t) / K, world)
+
     npart = len(lonf) * len(latf)
+    dt = timed(step_pinned)
+    m0 = dict(moved)
+    h0, d0 = D.transfer_bytes["h2d"], D.transfer_bytes["d2h"]
+    dt_np = timed(step_numpy)
     return {"value": world * npart / dt, "unit": UNIT,
-            "h2d_bytes_per_step": (D.transfer_bytes["h2d"] - h0) // K,
-            "d2h_bytes_per_step": (D.transfer_bytes["d2h"] - d0) // K,
-            "ms_per_step": dt * 1e3, "api": "numpy in / numpy out (pageable host memory)"}
+            "h2d_bytes_per_step": m0["h2d"] // (K + 2), "d2h_bytes_per_step": m0["d2h"] // (K + 2),
+            "ms_per_step": dt * 1e3,
+            "api": "torch CUDA tensors through the public API; particle grid in from pinned "
+                   "host memory, ridge points out to pinned host memory",
+            "numpy_api": {"value": world * npart / dt_np, "ms_per_step": dt_np * 1e3,
+                          "h2d_bytes_per_step": (D.transfer_bytes["h2d"] - h0) // (K + 2),
+                          "d2h_bytes_per_step": (D.transfer_bytes["d2h"] - d0) // (K + 2),
+                          "api": "numpy in / numpy out per call (pageable host memory)"}}
 
 
 def cpu_sample_rate(wl, rtol, atol, budget_s, threads):
     """Oracle particles/s on the host cores over a bounded sample of the grid.
 
     Integrates every `stride`-th longitude row (all latitudes) with the oracle's
-    DOP853 + spline RHS, then adds the per-particle cost of the oracle's
-    FTLE / eigen / ridge stencils measured on the full field."""
+    DOP853 + spline RHS, `reps` times over until the budget is spent (the
+    whole grid takes about a second on 16 cores), then adds the per-particle
+    cost of the oracle's FTLE / eigen / ridge stencils measured on the full
+    field."""
     import oracle
     oracle.build()
     of = oracle.spline_flow(wl["grid"], wl["Cu"], wl["Cv"], spherical=1)
@@ -802,10 +836,15 @@ def cpu_sample_rate(wl, rtol, atol, budget_s, threads):
     stride = max(1, nx // nrows)
     sample = lonf[::stride]
     t = time.perf_counter()
-    fm = oracle.flowmap_grid_2D(of, wl["t0"], wl["T"], sample, latf, wl["params"], rtol=rtol,
-                                atol=atol, nthreads=threads)
-    t_fm = time.perf_counter() - t
-    n_sample = len(sample) * len(latf)
+    reps = 0
+    while True:
+        fm = oracle.flowmap_grid_2D(of, wl["t0"], wl["T"], sample, latf, wl["params"], rtol=rtol,
+                                    atol=atol, nthreads=threads)
+        reps += 1
+        t_fm = time.perf_counter() - t
+        if t_fm * (reps + 1) / reps > budget_s:
+            break
+    n_sample = reps * len(sample) * len(latf)
     # stencil stages on a full-size field (cheap): reuse the sample rows tiled
     full = np.resize(fm, (nx, len(latf), 2))
     t = time.perf_counter()
@@ -814,16 +853,16 @@ def cpu_sample_rate(wl, rtol, atol, budget_s, threads):
     oracle.ftle_ridge_pts(f, np.ascontiguousarray(vec[..., :, 1]), lonf, latf, 0.0, wl["pct"])
     t_st = time.perf_counter() - t
     per_particle = t_fm / n_sample + t_st / (nx * len(latf))
-    return 1.0 / per_particle, n_sample, stride, t_fm + t_st
+    return 1.0 / per_particle, n_sample, stride, t_fm + t_st, reps
 
 
 def run_cpu_baseline(wl, rtol, atol, budget_s, value_gpu=None):
     threads = os.cpu_count() or 1
-    rate, n, stride, secs = cpu_sample_rate(wl, rtol, atol, budget_s, threads)
+    rate, n, stride, secs, reps = cpu_sample_rate(wl, rtol, atol, budget_s, threads)
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d particles (every %d-th lon row x all 251 lat) integrated by the C "
-                      "oracle (DOP853 + tricubic spline, OpenMP) + full-field FTLE/eig/ridge "
-                      "stencils; %.1f s of CPU work; %s" % (n, stride, secs, cpu_model()),
+            "sample": "%d particles (every %d-th lon row x all 251 lat, %d passes) integrated by "
+                      "the C oracle (DOP853 + tricubic spline, OpenMP) + full-field FTLE/eig/ridge "
+                      "stencils; %.1f s of CPU work; %s" % (n, stride, reps, secs, cpu_model()),
             "rtol": rtol}
 
 
@@ -841,20 +880,24 @@ def run_reference(args, rank, world):
     wl = dict(grid=grid, Cu=Cu, Cv=Cv, lonf=lonf, latf=latf, t0=180.0, T=W.GEO_T,
               pct=W.GEO_PERCENTILE, params=np.array([-1.0]), dx=lonf[1] - lonf[0],
               dy=latf[1] - latf[0])
-    rtol, atol = 1e-6, 1e-8
+    # the tolerance the accuracy ladder selects for the FP64 path on this
+    # workload (the loosest rtol within the flow-map error bound)
+    rtol = args.rtol or 1e-7
+    atol = 1e-2 * rtol
     budget = max(2.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         cpu_sample_rate(wl, rtol, atol, budget, os.cpu_count())
     rates, secs = [], 0.0
-    n = stride = 0
+    n = stride = reps = 0
     for _ in range(args.steps):
-        r, n, stride, s = cpu_sample_rate(wl, rtol, atol, budget, os.cpu_count())
+        r, n, stride, s, reps = cpu_sample_rate(wl, rtol, atol, budget, os.cpu_count())
         rates.append(r)
         secs += s
     value = statistics.median(rates)
     cores = os.cpu_count()
-    sample = ("%d particles (every %d-th lon row) per step, C restatement of the reference's "
-              "numba path (numba/numbalsoda/interpolation not installable), %s" % (n, stride, cpu_model()))
+    sample = ("%d particles (every %d-th lon row, %d passes) per step, C restatement of the "
+              "reference's numba path (numba/numbalsoda/interpolation not installable), %s"
+              % (n, stride, reps, cpu_model()))
     del torch
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * 169676 / value, "higher_is_better": True,
