@@ -129,32 +129,49 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    // last block: find the digit whose cumulative count passes `rank`
-    __shared__ unsigned int part[kSelThreads];
+    // last block: find the digit whose cumulative count passes `rank`.  Each
+    // thread sums `per` consecutive bins, a block-wide scan of those sums
+    // finds the one thread whose range holds the rank, and that thread walks
+    // its own bins (no serial loop over the whole block).
+    __shared__ long long wsum[kSelThreads / 32];
+    const long long rank = s->st.rank;
     const int nb = (int)dmask + 1;
     const int per = (nb + blockDim.x - 1) / blockDim.x;
-    unsigned int local = 0;
+    long long local = 0;
     for (int q = 0; q < per; ++q) {
         int b = threadIdx.x * per + q;
         if (b < nb) local += __ldcg(&s->hist[b]);
     }
-    part[threadIdx.x] = local;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    long long incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        long long v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[warp] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        long long rank = s->st.rank, cum = 0;
-        int t = 0;
-        for (; t < (int)blockDim.x; ++t) {
-            if (cum + (long long)part[t] > rank) break;
-            cum += part[t];
+    if (warp == 0) {
+        long long w = lane < nw ? wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            long long v = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += v;
         }
-        int b = t * per;
+        if (lane < nw) wsum[lane] = w;
+    }
+    __syncthreads();
+    if (warp) incl += wsum[warp - 1];
+    const long long excl = incl - local, total = wsum[nw - 1];
+    const bool beyond = rank >= total;  // unreachable for a valid rank
+    if ((excl <= rank && rank < incl) || (beyond && threadIdx.x == blockDim.x - 1)) {
+        long long cum = beyond ? total : excl;
+        int b = beyond ? nb : (int)threadIdx.x * per;
         unsigned int hb = 0;
         for (; b < nb; ++b) {
             hb = __ldcg(&s->hist[b]);
             if (cum + (long long)hb > rank) break;
             cum += hb;
         }
-        if (b >= nb) b = nb - 1;  // unreachable for a valid rank
+        if (b >= nb) b = nb - 1;
         s->st.rank = rank - cum;
         s->st.prefix = prefix | ((unsigned long long)b << shift);
         s->st.pmask = pmask | ((unsigned long long)dmask << shift);
@@ -226,7 +243,8 @@ sel_final_kernel(const double* __restrict__ f, long n, SelScratch* s, int mode, 
 
 static unsigned sel_grid(long n)
 {
-    long b = (n + kSelThreads * 8 - 1) / (kSelThreads * 8);
+    // two keys per thread before the grid reaches 4 blocks per SM
+    long b = (n + kSelThreads * 2 - 1) / (kSelThreads * 2);
     long cap = (long)sm_count() * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
@@ -272,8 +290,18 @@ static int percentile_enqueue(const double* f, long n, double q, double* out, Se
 // ------------------------------------------------------------ ridges
 
 constexpr int kRidgeThreads = 256;
-constexpr int kRidgeRounds = 8;
-constexpr int kRidgeTile = kRidgeThreads * kRidgeRounds;  // points per block
+constexpr int kRidgeRounds = 8;                            // most rounds per block
+constexpr int kRidgeTile = kRidgeThreads * kRidgeRounds;  // most points per block
+constexpr long kRidgeFillBlocks = 1216;                    // 8 blocks on each of 152 SMs
+
+// Rounds of kRidgeThreads points per block: fewer on small fields, so that the
+// grid still fills the GPU (a 676 x 251 field at 8 rounds would be 83 blocks,
+// each running 8 dependent rounds of the FP64 stencil).
+static inline int ridge_rounds(long n)
+{
+    long r = (n + kRidgeFillBlocks * kRidgeThreads - 1) / (kRidgeFillBlocks * kRidgeThreads);
+    return r < 1 ? 1 : (r > kRidgeRounds ? kRidgeRounds : (int)r);
+}
 
 struct RidgeIn {
     const double* f;
@@ -285,6 +313,7 @@ struct RidgeIn {
     const double* fmin_ptr;  // device threshold (percentile) or NULL
     double fmin_val;         // threshold when fmin_ptr is NULL
     double dx, dy;           // grid spacing; NaN: x[1] - x[0], y[1] - y[0] (ridges.py:39-40)
+    int rounds;              // rounds of kRidgeThreads points per block (ridge_rounds)
 };
 
 __device__ __forceinline__ void ridge_spacing(const RidgeIn& R, double* dx, double* dy)
@@ -344,10 +373,10 @@ ridge_flag_kernel(RidgeIn R, uint8_t* __restrict__ mask, double2* __restrict__ r
     double dx, dy;
     ridge_spacing(R, &dx, &dy);
     const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
-    const long base = (long)blockIdx.x * kRidgeTile;
+    const long base = (long)blockIdx.x * R.rounds * kRidgeThreads;
     unsigned int c = 0;
 #pragma unroll 1
-    for (int r = 0; r < kRidgeRounds; ++r) {
+    for (int r = 0; r < R.rounds; ++r) {
         long k = base + (long)r * kRidgeThreads + threadIdx.x;
         if (k >= n) break;
         double px = 0.0, py = 0.0;
@@ -402,11 +431,11 @@ ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
     double dx, dy;
     ridge_spacing(R, &dx, &dy);
     const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
-    const long base = (long)blockIdx.x * kRidgeTile;
+    const long base = (long)blockIdx.x * R.rounds * kRidgeThreads;
     unsigned long long run = off[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll 1
-    for (int r = 0; r < kRidgeRounds; ++r) {
+    for (int r = 0; r < R.rounds; ++r) {
         long k = base + (long)r * kRidgeThreads + threadIdx.x;
         bool on = k < n && mask[k];
         unsigned int bal = __ballot_sync(0xffffffffu, on);
@@ -454,7 +483,8 @@ extern "C" int nbcs_percentile(const double* f, int64_t n, double q, double* out
 static long ridge_blocks(int32_t nx, int32_t ny)
 {
     long n = (long)nx * ny;
-    return (n + kRidgeTile - 1) / kRidgeTile;
+    long per = (long)ridge_rounds(n) * kRidgeThreads;
+    return (n + per - 1) / per;
 }
 
 extern "C" size_t nbcs_ridge_scratch_bytes(int32_t nx, int32_t ny)
@@ -505,6 +535,7 @@ static int ridge_run(const double* f, const double* evec_max, const double* x, i
     R.sdd = sdd_thresh;
     R.dx = dx;
     R.dy = dy;
+    R.rounds = ridge_rounds(n);
     R.fmin_ptr = nullptr;
     R.fmin_val = use_percentile ? 0.0 : f_min;
     if (use_percentile && percentile != 0.0) {  // ridges.py:48-51
@@ -566,7 +597,12 @@ extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, cons
 namespace nbcs {
 
 constexpr size_t align256c(size_t b) { return (b + 255) & ~(size_t)255; }
-constexpr long kNoallocBlocks = (NBCS_RIDGE_NOALLOC_MAX_POINTS + kRidgeTile - 1) / kRidgeTile;
+// ridge_blocks() is at most kRidgeFillBlocks + 1 below 8 rounds, n / kRidgeTile
+// rounded up at 8 rounds
+constexpr long kNoallocBlocks =
+    (NBCS_RIDGE_NOALLOC_MAX_POINTS + kRidgeTile - 1) / kRidgeTile > kRidgeFillBlocks + 1
+        ? (NBCS_RIDGE_NOALLOC_MAX_POINTS + kRidgeTile - 1) / kRidgeTile
+        : kRidgeFillBlocks + 1;
 constexpr size_t kNoallocScratchBytes =
     align256c(sizeof(SelScratch)) + align256c(sizeof(unsigned int) * kNoallocBlocks) +
     align256c(sizeof(unsigned long long) * kNoallocBlocks) +
