@@ -596,6 +596,19 @@ def run_learned_eval(sp, rtol, atol, nx_ny=(4001, 2001), t0s=(168.0, 192.0, 216.
     out["speedup"] = out["learned"]["particles_per_s"] / out["plain"]["particles_per_s"]
     out["flowmap_diff_vs_plain_deg"] = {"mean": float(d.mean()), "q99": float(d[int(0.99 * d.numel())]),
                                         "max": float(d[-1])}
+    # error against an FP64 truth (rtol 1e-12) on every 8th particle of each
+    # axis at the first t0
+    xs, ys = x[::8].contiguous(), y[::8].contiguous()
+    truth = nb.flowmap_grid_2D(fl, t0s[0], W.GEO_T, xs, ys, p, rtol=1e-12, atol=1e-14,
+                               return_status=True)[0]
+    out["error_vs_truth_deg"] = {"particles": xs.numel() * ys.numel(), "t0": t0s[0]}
+    for name, kw in (("plain", {}), ("learned", {"step_model": sp, "step_model_mode": mode})):
+        fm = nb.flowmap_grid_2D(fl, t0s[0], W.GEO_T, xs, ys, p, rtol=rtol, atol=atol,
+                                precision="mixed", return_status=True, **kw)[0]
+        e = (fm - truth).abs().amax(-1).flatten().sort().values
+        out["error_vs_truth_deg"][name] = {"mean": float(e.mean()),
+                                           "q99": float(e[int(0.99 * e.numel())]),
+                                           "max": float(e[-1])}
     return out
 
 
