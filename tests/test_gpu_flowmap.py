@@ -219,3 +219,34 @@ def test_status_codes(nb):
     fm0 = nb.flowmap_grid_2D(fl, 0.0, 0.0, x, y, p)
     X, Y = np.meshgrid(x, y, indexing="ij")
     assert np.array_equal(fm0, np.stack([X, Y], -1))
+
+
+@pytest.mark.parametrize("shape", [(0, 5), (1, 7), (9, 1), (1, 1)])
+def test_flowmap_degenerate_grids(nb, orc, shape):
+    """Empty, single-row, single-column and single-point grids: the shapes the
+    reference's prange loop returns; FP64 flow maps within the double-gyre
+    parity bound of the oracle's (the RHS calls CUDA's sin / cos), the FTLE
+    of the same flow map bit-identical (all zero: no interior points)."""
+    nx, ny = shape
+    x, y = np.linspace(0.1, 1.9, nx), np.linspace(0.1, 0.9, ny)
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    for prec in ("fp64", "mixed"):
+        fm, st = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, precision=prec, return_status=True)
+        assert fm.shape == (nx, ny, 2) and st.shape == (nx, ny)
+        assert (st == 0).all()
+    fm = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p)
+    ofm = orc.flowmap_grid_2D(orc.double_gyre(), 0.0, 8.0, x, y, p)
+    assert fm.shape == ofm.shape and (fm.size == 0 or np.abs(fm - ofm).max() <= 2e-6)
+    f = nb.ftle_grid_2D(fm, 8.0, 0.1, 0.1)
+    assert f.shape == (nx, ny) and np.array_equal(f, orc.ftle_grid_2D(fm, 8.0, 0.1, 0.1))
+
+
+def test_flowmap_all_masked(nb):
+    x, y = np.linspace(0.1, 1.9, 12), np.linspace(0.1, 0.9, 6)
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    mask = np.ones((12, 6), bool)
+    for prec in ("fp64", "mixed"):
+        fm, st = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, mask=mask, precision=prec,
+                                    return_status=True)
+        assert np.array_equal(fm, np.zeros((12, 6, 2)))
+        assert (st == st.flat[0]).all() and st.flat[0] != 0
