@@ -177,7 +177,7 @@ typedef struct nbcs_batch {
     int32_t nflows, nfields, precision, reserved;
     int64_t total_chunks; /* 32-particle work units over all fields */
     int64_t ftle_blocks;  /* 256-point FTLE work units */
-    int64_t tiles;        /* particle tiles of one 128-thread block over all fields */
+    int64_t tiles;        /* particle tiles of one 256-thread block over all fields */
 } nbcs_batch;
 
 size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields);

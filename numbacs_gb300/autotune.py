@@ -2,8 +2,8 @@
 
 The persistent batched integrator's grid (blocks per SM) and the single-field
 mixed integrator's lanes per particle / grid cap trade occupancy against
-register and shared-memory use (stage derivatives take 12 KB of shared memory
-per 128-thread block; the spline RHS spends 64-96 registers per thread).  The
+register and shared-memory use (stage derivatives take 96 B of shared memory
+per thread; the spline RHS spends 64-96 registers per thread).  The
 best point depends on the flow and the particle count, so it is measured:
 each candidate is timed with CUDA events on the real workload, and the winner
 is cached in ``_build/autotune.json`` keyed by GPU, precision, flow kinds and

@@ -20,7 +20,9 @@ namespace nbcs {
 __global__ void batch_reset_kernel(BatchHeader* hdr) { hdr->counter = 0ull; }
 
 // Integrate particle (i, j) of field F and write its flow map and status
-// (the group's leader lane writes).  `lane` is the thread's lane in its warp.
+// (the group's leader lane writes).  `lane` is the thread's lane in its warp;
+// KS is the block size (the stride of the stage-derivative column kc).
+template <int KS>
 __device__ __forceinline__ void batch_solve32(const DevFlow32* __restrict__ flows,
                                               const DevField& F, int i, int j, int lane,
                                               float2* kc, int nmax)
@@ -38,16 +40,19 @@ __device__ __forceinline__ void batch_solve32(const DevFlow32* __restrict__ flow
         const DevFlow32& fl = flows[F.flow];
         switch (fl.kind) {
         case NBCS_FLOW_DOUBLE_GYRE:
-            st = dop853_solve32(FlowDG32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
+            st = dop853_solve32<FlowDG32, KS>(FlowDG32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a,
+                                              &rj, &nf);
             break;
         case NBCS_FLOW_BICKLEY:
-            st = dop853_solve32(FlowBickley32{}, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj,
-                                &nf);
+            st = dop853_solve32<FlowBickley32, KS>(FlowBickley32{}, P, xs, xe, yv, rtol, atol,
+                                                   nmax, kc, &a, &rj, &nf);
             break;
         default:  // spline fields run two lanes per particle
 #define NBCS_SPLINE_SOLVE(SPH, LP)                                                              \
-    st = dop853_solve32(FlowSpline32<SPH, LP>{fl.g, fl.c, fl.deg_per_km}, P, xs, xe, yv, rtol,  \
-                    atol, nmax, kc, &a, &rj, &nf)
+    st = dop853_solve32<FlowSpline32<SPH, LP>, KS>(FlowSpline32<SPH, LP>{fl.g, fl.c,           \
+                                                                        fl.deg_per_km},     \
+                                                   P, xs, xe, yv, rtol, atol, nmax, kc, &a,   \
+                                                   &rj, &nf)
             if (F.lp == 2) {
                 if (fl.spherical == 1) NBCS_SPLINE_SOLVE(1, 2);
                 else if (fl.spherical == 2) NBCS_SPLINE_SOLVE(2, 2);
@@ -87,26 +92,33 @@ batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
         const DevField& F = fields[f];
         int i, j;
         if (!batch_particle(F, (long long)c, lane, &i, &j)) continue;  // whole lane group
-        batch_solve32(flows, F, i, j, lane, kc, nmax);
+        batch_solve32<kThreads32>(flows, F, i, j, lane, kc, nmax);
     }
 }
 
 // tile schedule: block b integrates block tile b of the concatenated fields
-// (the single-field kernel's (TI x 8) tiles and warp sub-tiles); the hardware
-// block scheduler starts a new tile wherever one finishes
-__global__ void __launch_bounds__(kBatchThreads)
+// (the single-field kernel's block size, tiles and warp sub-tiles: 16 x 8
+// particles per block at two lanes a particle); the hardware block scheduler
+// starts a new tile wherever one finishes.  One kernel holds every flow kind,
+// which takes 128 registers a thread without spills: 2 resident blocks (16
+// geophysical fields at 0.4 deg: 22.2 ms; 128-thread blocks 22.4 ms; a
+// 3-block bound spills and takes 24.5 ms).
+constexpr int kBatchTileThreads = 256;
+constexpr int kBatchTileMinBlocks = 2;
+
+__global__ void __launch_bounds__(kBatchTileThreads, kBatchTileMinBlocks)
 batch32_tiles_kernel(const DevFlow32* __restrict__ flows, const DevField* __restrict__ fields,
                      int nfields, int nmax)
 {
-    __shared__ float2 ks[12 * kThreads32];
+    __shared__ float2 ks[12 * kBatchTileThreads];
     float2* kc = ks + threadIdx.x;
     const long long b = blockIdx.x;
     const DevField& F = fields[batch_find<kByTile>(fields, nfields, b)];
-    const long t = (long)(b - F.tile0) * kThreads32 + threadIdx.x;
+    const long t = (long)(b - F.tile0) * kBatchTileThreads + threadIdx.x;
     int i, j;
-    const bool ok = F.lp == 2 ? tile_particle<2>(t, F.nx, F.ny, &i, &j)
-                              : tile_particle<1>(t, F.nx, F.ny, &i, &j);
-    if (ok) batch_solve32(flows, F, i, j, threadIdx.x & 31, kc, nmax);
+    const bool ok = F.lp == 2 ? tile_particle<2, kBatchTileThreads>(t, F.nx, F.ny, &i, &j)
+                              : tile_particle<1, kBatchTileThreads>(t, F.nx, F.ny, &i, &j);
+    if (ok) batch_solve32<kBatchTileThreads>(flows, F, i, j, threadIdx.x & 31, kc, nmax);
 }
 
 static int persistent_blocks(const void* kernel, int threads, int blocks_per_sm)
@@ -136,7 +148,8 @@ int launch_batch32_tiles(const DevFlow32* flows, const DevField* fields, int nfi
                          long long tiles, int nmax, cudaStream_t s)
 {
     if (tiles > 0x7fffffffLL) return set_error(NBCS_ERR_UNSUPPORTED, "batch: too many tiles");
-    batch32_tiles_kernel<<<(unsigned)tiles, kBatchThreads, 0, s>>>(flows, fields, nfields, nmax);
+    batch32_tiles_kernel<<<(unsigned)tiles, kBatchTileThreads, 0, s>>>(flows, fields, nfields,
+                                                                       nmax);
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
@@ -229,8 +242,10 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         const int tj = batch_tile_j(D.lp);
         chunks += (long long)((F.nx + kBatchTileI - 1) / kBatchTileI) * ((F.ny + tj - 1) / tj);
         if (F.ftle) blocks += (n + kFtleBlock - 1) / kFtleBlock;
-        const int ti = kThreads32 / D.lp / 8;  // block tile: (ti x 8) particles
-        tiles += (long long)((F.nx + ti - 1) / ti) * ((F.ny + 7) / 8);
+        // block tile of the tile schedule: (ti x tj) particles
+        const int ti = D.lp == 2 ? TileShape<2, kBatchTileThreads>::TI : TileShape<1, kBatchTileThreads>::TI;
+        const int tjt = D.lp == 2 ? TileShape<2, kBatchTileThreads>::TJ : TileShape<1, kBatchTileThreads>::TJ;
+        tiles += (long long)((F.nx + ti - 1) / ti) * ((F.ny + tjt - 1) / tjt);
     }
     hdr->counter = 0;
     hdr->total_chunks = chunks;

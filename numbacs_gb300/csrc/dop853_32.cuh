@@ -100,14 +100,15 @@ __device__ __forceinline__ float f2_minus(F2 a, F2 b)  // (a - b) rounded to flo
 }
 
 // Stage argument combination sum_{j<S} a_Sj k_j for a compile-time stage S:
-// exactly S terms, the tableau entries as constant-bank operands.
-template <int S>
+// exactly S terms, the tableau entries as constant-bank operands.  KS is the
+// stride of the shared-memory column of stage derivatives (the block size).
+template <int S, int KS>
 __device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* a1)
 {
     float x = 0.f, y = 0.f;
 #pragma unroll
     for (int j = 0; j < S; ++j) {
-        const float2 kj = kc[j * kThreads32];
+        const float2 kj = kc[j * KS];
         x = fmaf(kA32[S][j], kj.x, x);
         y = fmaf(kA32[S][j], kj.y, y);
     }
@@ -117,28 +118,29 @@ __device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* 
 
 // The same for a runtime stage s that is uniform across the warp (one branch
 // of a jump table instead of eleven predicated terms per stage).
+template <int KS>
 __device__ __forceinline__ void stage_combo(int s, const float2* kc, float* a0, float* a1)
 {
     switch (s) {
     case 0: *a0 = 0.f; *a1 = 0.f; break;
-    case 1: stage_combo<1>(kc, a0, a1); break;
-    case 2: stage_combo<2>(kc, a0, a1); break;
-    case 3: stage_combo<3>(kc, a0, a1); break;
-    case 4: stage_combo<4>(kc, a0, a1); break;
-    case 5: stage_combo<5>(kc, a0, a1); break;
-    case 6: stage_combo<6>(kc, a0, a1); break;
-    case 7: stage_combo<7>(kc, a0, a1); break;
-    case 8: stage_combo<8>(kc, a0, a1); break;
-    case 9: stage_combo<9>(kc, a0, a1); break;
-    case 10: stage_combo<10>(kc, a0, a1); break;
-    default: stage_combo<11>(kc, a0, a1); break;
+    case 1: stage_combo<1, KS>(kc, a0, a1); break;
+    case 2: stage_combo<2, KS>(kc, a0, a1); break;
+    case 3: stage_combo<3, KS>(kc, a0, a1); break;
+    case 4: stage_combo<4, KS>(kc, a0, a1); break;
+    case 5: stage_combo<5, KS>(kc, a0, a1); break;
+    case 6: stage_combo<6, KS>(kc, a0, a1); break;
+    case 7: stage_combo<7, KS>(kc, a0, a1); break;
+    case 8: stage_combo<8, KS>(kc, a0, a1); break;
+    case 9: stage_combo<9, KS>(kc, a0, a1); break;
+    case 10: stage_combo<10, KS>(kc, a0, a1); break;
+    default: stage_combo<11, KS>(kc, a0, a1); break;
     }
 }
 
 // Integrate one particle (y, as compensated pairs) over solver time [x, xend].
-// `kc` is this thread's shared-memory column of stage derivatives (stride
-// kThreads32).  Returns an NBCS_PARTICLE_* code.
-template <class Flow>
+// `kc` is this thread's shared-memory column of stage derivatives (stride KS,
+// the block size).  Returns an NBCS_PARTICLE_* code.
+template <class Flow, int KS = kThreads32>
 __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2* y, float rtol,
                               float atol, int nmax, float2* kc, int* acc, int* rej, int* nfcn)
 {
@@ -211,18 +213,18 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
         for (int s = 0; s < 12; ++s) {
             if (s == 0 && !fsal) continue;
             float a0, a1;
-            stage_combo(s, kc, &a0, &a1);
+            stage_combo<KS>(s, kc, &a0, &a1);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
             fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);
-            kc[s * kThreads32] = make_float2(kk[0], kk[1]);
+            kc[s * KS] = make_float2(kk[0], kk[1]);
         }
         fsal = false;
         *nfcn += 11;
         float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
 #pragma unroll
         for (int j = 0; j < 12; ++j) {
-            const float2 kj = kc[j * kThreads32];
+            const float2 kj = kc[j * KS];
             b[0] = fmaf(kB32[j], kj.x, b[0]);
             b[1] = fmaf(kB32[j], kj.y, b[1]);
             e5[0] = fmaf(kE5_32[j], kj.x, e5[0]);
@@ -270,27 +272,35 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
     return status;
 }
 
-// Thread -> (particle group, lane) map.  A block of kThreads32 threads holds
-// kThreads32/LP particles laid out as a (TI x 8) tile of the grid; tiles run
-// in row-major order.  Inside the tile each warp takes a compact (WI x WJ)
+// Thread -> (particle group, lane) map for blocks of BT threads.  A block
+// holds BT/LP particles laid out as a (TI x TJ) tile of the grid; tiles run in
+// row-major order.  Inside the tile each warp takes a compact (WI x WJ)
 // sub-tile (4 x 8, 4 x 4, 2 x 4 particles at LP = 1, 2, 4): the fewer spline
 // cells a warp's particles sit in, the more of its stencil gathers hit the
-// same 32-byte entries.
-template <int LP>
+// same 32-byte entries.  Blocks of two or more warps use tiles TJW wide in y
+// (8 unless given; never narrower than a warp's sub-tile).
+template <int LP, int BT, int TJW = 8>
+struct TileShape {
+    static constexpr int PW = 32 / LP;                   // particles per warp
+    static constexpr int WJ = LP == 1 ? 8 : 4, WI = PW / WJ;
+    static constexpr int PB = BT / LP;                   // particles per block
+    static constexpr int TJ = BT >= 64 && TJW > WJ ? TJW : WJ, TI = PB / TJ;
+    static constexpr int WPJ = TJ / WJ;                  // warps along j
+    static_assert(BT % 32 == 0 && TJ % WJ == 0 && PB % TJ == 0, "tile shape");
+};
+
+template <int LP, int BT = kThreads32, int TJW = 8>
 __device__ __forceinline__ bool tile_particle(long t, int nx, int ny, int* i, int* j)
 {
-    constexpr int PB = kThreads32 / LP, TJ = 8, TI = PB / TJ;
-    constexpr int PW = 32 / LP;                     // particles per warp
-    constexpr int WJ = LP == 1 ? 8 : 4, WI = PW / WJ;
-    constexpr int WPJ = TJ / WJ;                    // warps along j
-    long tile = t / kThreads32;
-    int r = (int)(t - tile * kThreads32) / LP;
-    int w = r / PW, q = r - w * PW;
-    int tiles_j = (ny + TJ - 1) / TJ;
+    using S = TileShape<LP, BT, TJW>;
+    long tile = t / BT;
+    int r = (int)(t - tile * BT) / LP;
+    int w = r / S::PW, q = r - w * S::PW;
+    int tiles_j = (ny + S::TJ - 1) / S::TJ;
     long ti = tile / tiles_j;
     int tj = (int)(tile - ti * tiles_j);
-    *i = (int)(ti * TI) + (w / WPJ) * WI + q / WJ;
-    *j = tj * TJ + (w % WPJ) * WJ + q % WJ;
+    *i = (int)(ti * S::TI) + (w / S::WPJ) * S::WI + q / S::WJ;
+    *j = tj * S::TJ + (w % S::WPJ) * S::WJ + q % S::WJ;
     return *i < nx && *j < ny;
 }
 

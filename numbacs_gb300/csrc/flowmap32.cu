@@ -21,9 +21,21 @@
 
 namespace nbcs {
 
+// Threads per block of the single-field integrator, and the width in y of the
+// particle tile a block integrates: at LP = 2 a block takes a 16 x 8 tile of
+// the grid (8 warps, each a 4 x 4 sub-tile).  Measured on the geophysical
+// spline workload (676 x 251 particles): 128-thread 8 x 8 tiles 5.52 ms,
+// 256-thread 16 x 8 tiles 5.24 ms, 8 x 16 tiles 5.36 ms, 32 x 4 tiles 5.43
+// ms; warps of one block share L1 lines of neighbouring trajectories, and the
+// flow is mostly zonal.  The minimum of 3 resident blocks gives the compiler
+// 85 registers a thread; it takes 80 with no spills (24 warps per SM), 5.08
+// ms; a 64-register cap with 4 blocks spilled and took 5.40 ms.
+constexpr int kFm32Block = 256;
+constexpr int kFm32TileJ = 8;
+constexpr int kFm32MinBlocks = 3;
 
 template <class Flow>
-__global__ void __launch_bounds__(kThreads32)
+__global__ void __launch_bounds__(kFm32Block, kFm32MinBlocks)
 flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restrict__ x,
                  const double* __restrict__ y, int nx, int nyv, AuxGrid aux,
                  const uint8_t* __restrict__ mask, double* __restrict__ out,
@@ -31,20 +43,21 @@ flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restr
                  float atol, int nmax, long nthreads)
 {
     constexpr int LP = Flow::LP;
-    __shared__ float2 ks[12 * kThreads32];
+    __shared__ float2 ks[12 * kFm32Block];
     float2* kc = ks + threadIdx.x;
     const F2 xs = f2_from_double(ts), xe = f2_from_double(te);
-    // every lane of a group walks the same trip count (nthreads is a multiple of kThreads32)
+    // every lane of a group walks the same trip count (nthreads is a multiple of kFm32Block)
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nthreads;
          t += (long)gridDim.x * blockDim.x) {
         int i, j;
-        if (!tile_particle<LP>(t, nx, nyv, &i, &j)) continue;
+        if (!tile_particle<LP, kFm32Block, kFm32TileJ>(t, nx, nyv, &i, &j)) continue;
         long k = (long)i * nyv + j;
         double r0 = 0.0, r1 = 0.0, x0, y0;
         int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
         if (particle_start(aux, x, y, mask, nx, i, j, &x0, &y0)) {
             F2 yv[2] = {f2_from_double(x0), f2_from_double(y0)};
-            st = dop853_solve32(fl, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
+            st = dop853_solve32<Flow, kFm32Block>(fl, P, xs, xe, yv, rtol, atol, nmax, kc, &a,
+                                                  &rj, &nf);
             r0 = f2_to_double(yv[0]);
             r1 = f2_to_double(yv[1]);
         }
@@ -132,18 +145,16 @@ struct Launch32 {
     template <class Flow>
     int operator()(const Flow& fl) const
     {
-        constexpr int LP = Flow::LP;
-        constexpr int PB = kThreads32 / LP;  // particles per block
-        constexpr int TI = PB / 8;
-        long tiles = (long)((a->nx + TI - 1) / TI) * ((a->nyv() + 7) / 8);
-        long nthreads = tiles * kThreads32;
+        using S = TileShape<Flow::LP, kFm32Block, kFm32TileJ>;
+        long tiles = (long)((a->nx + S::TI - 1) / S::TI) * ((a->nyv() + S::TJ - 1) / S::TJ);
+        long nthreads = tiles * kFm32Block;
         long blocks = tiles;
         if (a->blocks_per_sm > 0) {
             long cap = (long)sm_count() * a->blocks_per_sm;
             if (blocks > cap) blocks = cap;
         }
         if (blocks > (1L << 30)) blocks = 1L << 30;
-        flowmap32_kernel<<<(unsigned)blocks, kThreads32, 0, a->stream>>>(
+        flowmap32_kernel<<<(unsigned)blocks, kFm32Block, 0, a->stream>>>(
             fl, to_float(a->P), a->ts, a->te, a->x, a->y, a->nx, a->nyv(), a->aux, a->mask, a->out,
             a->status, a->stats, (float)a->rtol, (float)a->atol, a->nmax, nthreads);
         NBCS_LAUNCH_CHECK();

@@ -159,7 +159,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
 #pragma unroll 1
         for (int s = 1; s < 12; ++s) {
             float a0, a1;
-            stage_combo(s, kc, &a0, &a1);
+            stage_combo<kThreads32>(s, kc, &a0, &a1);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
             fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);

@@ -70,7 +70,7 @@ def test_batch_autotune_and_sizes(nb):
         tj = 4 if f.flow.kind == 2 else 8
         return -(-f.x.numel() // 4) * -(-f.y.numel() // tj)
     assert int(b.plan.total_chunks) == sum(units(f) for f in fields)
-    def tiles(f):  # one 128-thread block: (16 x 8) particles, (8 x 8) at two lanes each
-        ti = 8 if f.flow.kind == 2 else 16
+    def tiles(f):  # one 256-thread block: (32 x 8) particles, (16 x 8) at two lanes each
+        ti = 16 if f.flow.kind == 2 else 32
         return -(-f.x.numel() // ti) * -(-f.y.numel() // 8)
     assert int(b.plan.tiles) == sum(tiles(f) for f in fields)
