@@ -22,42 +22,68 @@
 namespace nbcs {
 
 #define F_(x) ((float)(x))
-// DP853 tableau, 0-based stage index: stage s uses kA32[s][j] for j < s.
-static __constant__ float kA32[12][12] = {
-    {0.f},
-    {F_(DP853_A_2_1)},
-    {F_(DP853_A_3_1), F_(DP853_A_3_2)},
-    {F_(DP853_A_4_1), F_(DP853_A_4_2), F_(DP853_A_4_3)},
-    {F_(DP853_A_5_1), F_(DP853_A_5_2), F_(DP853_A_5_3), F_(DP853_A_5_4)},
-    {F_(DP853_A_6_1), F_(DP853_A_6_2), F_(DP853_A_6_3), F_(DP853_A_6_4), F_(DP853_A_6_5)},
-    {F_(DP853_A_7_1), F_(DP853_A_7_2), F_(DP853_A_7_3), F_(DP853_A_7_4), F_(DP853_A_7_5),
-     F_(DP853_A_7_6)},
-    {F_(DP853_A_8_1), F_(DP853_A_8_2), F_(DP853_A_8_3), F_(DP853_A_8_4), F_(DP853_A_8_5),
-     F_(DP853_A_8_6), F_(DP853_A_8_7)},
-    {F_(DP853_A_9_1), F_(DP853_A_9_2), F_(DP853_A_9_3), F_(DP853_A_9_4), F_(DP853_A_9_5),
-     F_(DP853_A_9_6), F_(DP853_A_9_7), F_(DP853_A_9_8)},
-    {F_(DP853_A_10_1), F_(DP853_A_10_2), F_(DP853_A_10_3), F_(DP853_A_10_4), F_(DP853_A_10_5),
-     F_(DP853_A_10_6), F_(DP853_A_10_7), F_(DP853_A_10_8), F_(DP853_A_10_9)},
-    {F_(DP853_A_11_1), F_(DP853_A_11_2), F_(DP853_A_11_3), F_(DP853_A_11_4), F_(DP853_A_11_5),
-     F_(DP853_A_11_6), F_(DP853_A_11_7), F_(DP853_A_11_8), F_(DP853_A_11_9), F_(DP853_A_11_10)},
-    {F_(DP853_A_12_1), F_(DP853_A_12_2), F_(DP853_A_12_3), F_(DP853_A_12_4), F_(DP853_A_12_5),
-     F_(DP853_A_12_6), F_(DP853_A_12_7), F_(DP853_A_12_8), F_(DP853_A_12_9), F_(DP853_A_12_10),
-     F_(DP853_A_12_11)},
-};
-static __constant__ float kC32[12] = {0.f, F_(DP853_C_2), F_(DP853_C_3), F_(DP853_C_4), F_(DP853_C_5),
-                               F_(DP853_C_6), F_(DP853_C_7), F_(DP853_C_8), F_(DP853_C_9),
-                               F_(DP853_C_10), F_(DP853_C_11), 1.0f};
-static __constant__ float kB32[12] = {F_(DP853_B_1), F_(DP853_B_2), F_(DP853_B_3), F_(DP853_B_4),
-                               F_(DP853_B_5), F_(DP853_B_6), F_(DP853_B_7), F_(DP853_B_8),
-                               F_(DP853_B_9), F_(DP853_B_10), F_(DP853_B_11), F_(DP853_B_12)};
-static __constant__ float kE5_32[12] = {F_(DP853_E5_1), F_(DP853_E5_2), F_(DP853_E5_3), F_(DP853_E5_4),
+// DP853 tableau as compile-time FP32 values, 0-based stage index: stage s uses
+// a(s, j) for j < s.  Being constants of the compiler (not of a memory bank),
+// the zero entries (a_i2 for i > 3, a_i3 for i > 5, b_2..b_5, the error
+// weights at stages 2-5) cost neither a load of k_j nor an FMA.
+struct DP853F {
+    __host__ __device__ static constexpr float a(int s, int j)
+    {
+        constexpr float t[12][12] = {
+            {0.f},
+            {F_(DP853_A_2_1)},
+            {F_(DP853_A_3_1), F_(DP853_A_3_2)},
+            {F_(DP853_A_4_1), F_(DP853_A_4_2), F_(DP853_A_4_3)},
+            {F_(DP853_A_5_1), F_(DP853_A_5_2), F_(DP853_A_5_3), F_(DP853_A_5_4)},
+            {F_(DP853_A_6_1), F_(DP853_A_6_2), F_(DP853_A_6_3), F_(DP853_A_6_4), F_(DP853_A_6_5)},
+            {F_(DP853_A_7_1), F_(DP853_A_7_2), F_(DP853_A_7_3), F_(DP853_A_7_4), F_(DP853_A_7_5),
+             F_(DP853_A_7_6)},
+            {F_(DP853_A_8_1), F_(DP853_A_8_2), F_(DP853_A_8_3), F_(DP853_A_8_4), F_(DP853_A_8_5),
+             F_(DP853_A_8_6), F_(DP853_A_8_7)},
+            {F_(DP853_A_9_1), F_(DP853_A_9_2), F_(DP853_A_9_3), F_(DP853_A_9_4), F_(DP853_A_9_5),
+             F_(DP853_A_9_6), F_(DP853_A_9_7), F_(DP853_A_9_8)},
+            {F_(DP853_A_10_1), F_(DP853_A_10_2), F_(DP853_A_10_3), F_(DP853_A_10_4),
+             F_(DP853_A_10_5), F_(DP853_A_10_6), F_(DP853_A_10_7), F_(DP853_A_10_8),
+             F_(DP853_A_10_9)},
+            {F_(DP853_A_11_1), F_(DP853_A_11_2), F_(DP853_A_11_3), F_(DP853_A_11_4),
+             F_(DP853_A_11_5), F_(DP853_A_11_6), F_(DP853_A_11_7), F_(DP853_A_11_8),
+             F_(DP853_A_11_9), F_(DP853_A_11_10)},
+            {F_(DP853_A_12_1), F_(DP853_A_12_2), F_(DP853_A_12_3), F_(DP853_A_12_4),
+             F_(DP853_A_12_5), F_(DP853_A_12_6), F_(DP853_A_12_7), F_(DP853_A_12_8),
+             F_(DP853_A_12_9), F_(DP853_A_12_10), F_(DP853_A_12_11)},
+        };
+        return t[s][j];
+    }
+    __host__ __device__ static constexpr float b(int j)
+    {
+        constexpr float t[12] = {F_(DP853_B_1), F_(DP853_B_2), F_(DP853_B_3), F_(DP853_B_4),
+                                 F_(DP853_B_5), F_(DP853_B_6), F_(DP853_B_7), F_(DP853_B_8),
+                                 F_(DP853_B_9), F_(DP853_B_10), F_(DP853_B_11), F_(DP853_B_12)};
+        return t[j];
+    }
+    // 5th-order error weights
+    __host__ __device__ static constexpr float e5(int j)
+    {
+        constexpr float t[12] = {F_(DP853_E5_1), F_(DP853_E5_2), F_(DP853_E5_3), F_(DP853_E5_4),
                                  F_(DP853_E5_5), F_(DP853_E5_6), F_(DP853_E5_7), F_(DP853_E5_8),
-                                 F_(DP853_E5_9), F_(DP853_E5_10), F_(DP853_E5_11), F_(DP853_E5_12)};
-// 3rd-order estimate weights b_j - bhh_j (bhh at stages 1, 9, 12)
-static __constant__ float kE3_32[12] = {F_(DP853_B_1 - DP853_BHH1), F_(DP853_B_2), F_(DP853_B_3),
+                                 F_(DP853_E5_9), F_(DP853_E5_10), F_(DP853_E5_11),
+                                 F_(DP853_E5_12)};
+        return t[j];
+    }
+    // 3rd-order estimate weights b_j - bhh_j (bhh at stages 1, 9, 12)
+    __host__ __device__ static constexpr float e3(int j)
+    {
+        constexpr float t[12] = {F_(DP853_B_1 - DP853_BHH1), F_(DP853_B_2), F_(DP853_B_3),
                                  F_(DP853_B_4), F_(DP853_B_5), F_(DP853_B_6), F_(DP853_B_7),
                                  F_(DP853_B_8), F_(DP853_B_9 - DP853_BHH2), F_(DP853_B_10),
                                  F_(DP853_B_11), F_(DP853_B_12 - DP853_BHH3)};
+        return t[j];
+    }
+};
+// stage times c_s (a runtime stage index reads them from the constant bank)
+static __constant__ float kC32[12] = {0.f, F_(DP853_C_2), F_(DP853_C_3), F_(DP853_C_4), F_(DP853_C_5),
+                               F_(DP853_C_6), F_(DP853_C_7), F_(DP853_C_8), F_(DP853_C_9),
+                               F_(DP853_C_10), F_(DP853_C_11), 1.0f};
 #undef F_
 
 constexpr int kThreads32 = 128;
@@ -99,21 +125,57 @@ __device__ __forceinline__ float f2_minus(F2 a, F2 b)  // (a - b) rounded to flo
     return (a.hi - b.hi) + (a.lo - b.lo);
 }
 
-// Stage argument combination sum_{j<S} a_Sj k_j for a compile-time stage S:
-// exactly S terms, the tableau entries as constant-bank operands.  KS is the
-// stride of the shared-memory column of stage derivatives (the block size).
+// Terms j >= J of the stage argument combination sum_{j<S} a_Sj k_j: the
+// nonzero ones only, in ascending j.  KS is the stride of the shared-memory
+// column of stage derivatives (the block size).
+template <int S, int KS, int J = 0>
+__device__ __forceinline__ void stage_terms(const float2* kc, float& x, float& y)
+{
+    if constexpr (J < S) {
+        constexpr float a = DP853F::a(S, J);
+        if constexpr (a != 0.f) {
+            const float2 kj = kc[J * KS];
+            x = fmaf(a, kj.x, x);
+            y = fmaf(a, kj.y, y);
+        }
+        stage_terms<S, KS, J + 1>(kc, x, y);
+    }
+}
+
+// Stage argument combination for a compile-time stage S.
 template <int S, int KS>
 __device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* a1)
 {
     float x = 0.f, y = 0.f;
-#pragma unroll
-    for (int j = 0; j < S; ++j) {
-        const float2 kj = kc[j * KS];
-        x = fmaf(kA32[S][j], kj.x, x);
-        y = fmaf(kA32[S][j], kj.y, y);
-    }
+    stage_terms<S, KS>(kc, x, y);
     *a0 = x;
     *a1 = y;
+}
+
+// The step's solution increment sum b_j k_j and the two error estimates
+// sum e5_j k_j, sum e3_j k_j, over the stages with a nonzero weight.
+template <int KS, int J = 0>
+__device__ __forceinline__ void step_sums(const float2* kc, float* b, float* e5, float* e3)
+{
+    if constexpr (J < 12) {
+        constexpr float wb = DP853F::b(J), w5 = DP853F::e5(J), w3 = DP853F::e3(J);
+        if constexpr (wb != 0.f || w5 != 0.f || w3 != 0.f) {
+            const float2 kj = kc[J * KS];
+            if constexpr (wb != 0.f) {
+                b[0] = fmaf(wb, kj.x, b[0]);
+                b[1] = fmaf(wb, kj.y, b[1]);
+            }
+            if constexpr (w5 != 0.f) {
+                e5[0] = fmaf(w5, kj.x, e5[0]);
+                e5[1] = fmaf(w5, kj.y, e5[1]);
+            }
+            if constexpr (w3 != 0.f) {
+                e3[0] = fmaf(w3, kj.x, e3[0]);
+                e3[1] = fmaf(w3, kj.y, e3[1]);
+            }
+        }
+        step_sums<KS, J + 1>(kc, b, e5, e3);
+    }
 }
 
 // The same for a runtime stage s that is uniform across the warp (one branch
@@ -222,16 +284,7 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
         fsal = false;
         *nfcn += 11;
         float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
-#pragma unroll
-        for (int j = 0; j < 12; ++j) {
-            const float2 kj = kc[j * KS];
-            b[0] = fmaf(kB32[j], kj.x, b[0]);
-            b[1] = fmaf(kB32[j], kj.y, b[1]);
-            e5[0] = fmaf(kE5_32[j], kj.x, e5[0]);
-            e5[1] = fmaf(kE5_32[j], kj.y, e5[1]);
-            e3[0] = fmaf(kE3_32[j], kj.x, e3[0]);
-            e3[1] = fmaf(kE3_32[j], kj.y, e3[1]);
-        }
+        step_sums<KS>(kc, b, e5, e3);
         F2 ynew[2];
         float err = 0.f, err2 = 0.f;
 #pragma unroll

@@ -167,16 +167,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
         }
         *nfcn += 11;
         float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
-#pragma unroll
-        for (int j = 0; j < 12; ++j) {
-            const float2 kj = kc[j * kThreads32];
-            b[0] = fmaf(kB32[j], kj.x, b[0]);
-            b[1] = fmaf(kB32[j], kj.y, b[1]);
-            e5[0] = fmaf(kE5_32[j], kj.x, e5[0]);
-            e5[1] = fmaf(kE5_32[j], kj.y, e5[1]);
-            e3[0] = fmaf(kE3_32[j], kj.x, e3[0]);
-            e3[1] = fmaf(kE3_32[j], kj.y, e3[1]);
-        }
+        step_sums<kThreads32>(kc, b, e5, e3);
         F2 ynew[2];
         float err = 0.f, err2 = 0.f;
 #pragma unroll
