@@ -487,9 +487,13 @@ def run_batch(wl, rtol, steps):
             "blocks_per_sm": batch.blocks_per_sm, "ms_per_batch": ms_batch,
             "particles_per_s": n / (ms_batch * 1e-3), "fields_per_s": len(fields) / (ms_batch * 1e-3),
             "sequential_ms": ms_seq, "speedup_vs_sequential": ms_seq / ms_batch,
-            "schedule": ("one block per particle tile" if batch.blocks_per_sm < 0 else
+            "schedule": ("one block per particle tile" if batch.blocks_per_sm == -1 else
+                         "per-field launches on %d parallel streams, longest first"
+                         % batch.max_streams if batch.blocks_per_sm == -2 else
                          "persistent, %d blocks/SM, warps take chunks" % batch.blocks_per_sm),
-            "launch": "one integrator launch + one FTLE launch, CUDA graph replay"}
+            "launch": ("one CUDA graph: a per-field integrator + FTLE launch on each branch"
+                       if batch.blocks_per_sm == -2 else
+                       "one integrator launch + one FTLE launch, CUDA graph replay")}
 
 
 def train_proposer(rtol, atol, seeds=range(8), t0s=(168.0, 190.0, 215.0), sample=0.22):

@@ -62,9 +62,10 @@ def _time(fn, reps=2):
 
 def tune_batch(batch, candidates=None, force=False):
     """Schedule for a prepared FTLEBatch (cached): blocks per SM of the
-    persistent grid, or -1 for one block per particle tile (mixed only)."""
+    persistent grid, -1 for one block per particle tile (mixed only), or -2
+    for per-field launches on parallel streams."""
     if candidates is None:
-        candidates = (2, 3, 4, 5, 6, 8) + ((-1,) if batch.precision == "mixed" else ())
+        candidates = (2, 3, 4, 5, 6, 8, -2) + ((-1,) if batch.precision == "mixed" else ())
     kinds = sorted({(f.flow.kind, f.flow.spherical) for f in batch.fields})
     bucket = int(math.log2(max(1, batch.particles)))
     key = "batch/%s/%s/%s/%d" % (_gpu(), batch.precision, kinds, bucket)

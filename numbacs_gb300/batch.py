@@ -1,15 +1,18 @@
-"""Many FTLE fields in one persistent launch.
+"""Many FTLE fields in one CUDA graph.
 
 The reference builds FTLE time series with a Python loop over t0 that calls
 ``flowmap_grid_2D`` and ``ftle_grid_2D`` per field
 (examples/time_series/plot_dg_time_series.py,
 examples/time_series/plot_dg_numbacs_vs_scipy.py).  :class:`FTLEBatch` takes
 the whole list of fields -- any mix of flows, start times, integration
-lengths and grid sizes -- and integrates every particle of every field in one
-persistent kernel whose warps take 32-particle chunks from a shared counter
-(csrc/batch32.cu, csrc/batch64.cu), then computes all FTLE fields and their
-eigenvectors in one stencil launch.  The run is kernel launches only, so it is
-captured once in a CUDA graph and replayed.
+lengths and grid sizes -- and runs them under one of three schedules: one
+persistent kernel whose warps take 32-particle chunks from a shared counter,
+or one kernel with one block per particle tile of any field (csrc/batch32.cu,
+csrc/batch64.cu), each followed by one FTLE/eigenvector launch for all
+fields; or every field's own single-field integrator and FTLE launches spread
+over parallel streams, longest first, so that the tail of one field overlaps
+the start of the next.  The run is kernel launches only, so it is captured
+once in a CUDA graph and replayed.
 """
 import ctypes
 
@@ -52,17 +55,24 @@ class Field:
         return self.x.numel() * self.y.numel()
 
 
+STREAMS = -2  # schedule: one integrator + one FTLE launch per field on parallel streams
+
+
 class FTLEBatch:
     """A prepared batch of fields; ``run()`` recomputes every field in place.
 
     ``precision`` is "mixed" or "fp64"; ``blocks_per_sm`` picks the schedule:
     >= 0 a persistent grid of that many blocks per SM (0: full occupancy) whose
     warps take particle chunks from a shared counter, -1 (mixed) one block per
-    particle tile of any field; None takes it from the autotuner cache, tuning
-    on first use.  ``graph=True`` captures the run in a CUDA graph on first call.
+    particle tile of any field, -2 (``STREAMS``) each field's own single-field
+    integrator and FTLE launches, spread longest first over ``max_streams``
+    streams so that one field's tail overlaps the next field's start; None
+    takes it from the autotuner cache, tuning on first use.  ``graph=True``
+    captures the run (all streams) in a CUDA graph on first call.
     """
 
-    def __init__(self, fields, precision="mixed", blocks_per_sm=None, graph=True, max_steps=100000):
+    def __init__(self, fields, precision="mixed", blocks_per_sm=None, graph=True, max_steps=100000,
+                 max_streams=16):
         D.require_cuda()
         if precision not in _PREC:
             raise ValueError("precision must be 'fp64' or 'mixed'")
@@ -102,6 +112,11 @@ class FTLEBatch:
                                         len(self.fields), _PREC[precision], D.ptr(self._scratch),
                                         nbytes, ctypes.byref(self.plan), D.stream_ptr()))
         self.max_steps = int(max_steps)
+        self.max_streams = max(1, int(max_streams))
+        self._streams = None
+        # longest work first: particles x |T|
+        self._order = sorted(range(len(self.fields)),
+                             key=lambda k: -self.fields[k].particles * abs(self.fields[k].T))
         if blocks_per_sm is None:
             from .autotune import tune_batch
             blocks_per_sm = tune_batch(self)
@@ -122,8 +137,43 @@ class FTLEBatch:
 
     def launch(self, blocks_per_sm=None):
         """Enqueue one run on the current stream (no graph)."""
+        bps = self.blocks_per_sm if blocks_per_sm is None else int(blocks_per_sm)
+        if bps == STREAMS:
+            self._launch_streams()
+            return
         _lib.check(_lib.load().nbcs_batch_run(ctypes.byref(self.plan), self._opts(blocks_per_sm),
                                               D.stream_ptr()))
+
+    def _launch_streams(self):
+        """Every field through the single-field entry points (nbcs_flowmap_grid_2d,
+        nbcs_ftle_evec_2d) on its own stream of a small pool, forked from and
+        joined back into the current stream (capturable)."""
+        L = _lib.load()
+        main = torch.cuda.current_stream()
+        if self._streams is None:
+            self._streams = [torch.cuda.Stream() for _ in
+                             range(min(self.max_streams, len(self.fields)))]
+        for s in self._streams:
+            s.wait_stream(main)
+        o = _lib.NbcsOpts()
+        o.precision = _PREC[self.precision]
+        o.max_steps = self.max_steps
+        # two lanes a spline particle in the mixed path, as the other schedules
+        # (the lane count sets the FP32 summation order): identical results
+        o.lanes_per_particle = 2
+        for q, k in enumerate(self._order):
+            f = self.fields[k]
+            sp = ctypes.c_void_p(self._streams[q % len(self._streams)].cuda_stream)
+            nx, ny = f.x.numel(), f.y.numel()
+            _lib.check(L.nbcs_flowmap_grid_2d(
+                f.flow.struct, f.t0, f.T, D.ptr(f.x), nx, D.ptr(f.y), ny,
+                f.params.ctypes.data_as(_lib._vp), len(f.params), f.rtol, f.atol, D.ptr(f.mask),
+                D.ptr(f.flowmap), D.ptr(f.status), o, sp))
+            if f.ftle is not None:
+                _lib.check(L.nbcs_ftle_evec_2d(D.ptr(f.flowmap), nx, ny, f.T, f.dx, f.dy,
+                                               D.ptr(f.mask), D.ptr(f.ftle), D.ptr(f.evec), sp))
+        for s in self._streams:
+            main.wait_stream(s)
 
     def capture(self):
         """Capture one run into a CUDA graph (after one eager warm-up run)."""

@@ -37,7 +37,7 @@ def _fields(nb):
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("schedule", [3, -1])
+@pytest.mark.parametrize("schedule", [3, -1, -2])
 def test_batch_equals_single_field(nb, precision, graph, schedule):
     from numbacs_gb300.batch import FTLEBatch
     fields = _fields(nb)
