@@ -63,7 +63,8 @@ typedef struct nbcs_flow {
     const double* coef_uv;  /* SPLINE2D FP64 coefficients (device), required */
     /* SPLINE2D FP32 copy (device), required for NBCS_PREC_MIXED, in the "quad"
      * layout: entry k (32 bytes) holds u_j, v_j for j = k .. k+3 (zeros past the
-     * end); n entries, 32-byte aligned. */
+     * end); n entries, 32-byte aligned; n < 2^32 (the mixed path indexes
+     * entries with 32-bit integers). */
     const float* coef_uv32;
 } nbcs_flow;
 

@@ -62,6 +62,12 @@ int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int p
             return set_error(NBCS_ERR_INVALID, "mixed precision needs the FP32 coefficient copy");
         if (precision == NBCS_PREC_MIXED && (reinterpret_cast<uintptr_t>(flow->coef_uv32) & 31))
             return set_error(NBCS_ERR_INVALID, "the FP32 coefficient copy must be 32-byte aligned");
+        // the mixed path indexes quad entries with 32-bit integers
+        if (precision == NBCS_PREC_MIXED &&
+            (flow->grid[2] + 2.0) * (flow->grid[5] + 2.0) * (flow->grid[8] + 2.0) >= 4294967296.0)
+            return set_error(NBCS_ERR_UNSUPPORTED,
+                             "mixed precision: spline grids of 2^32 nodes or more (with the "
+                             "2-node border) are not supported; use precision fp64");
         break;
     }
     default:

@@ -80,10 +80,14 @@ struct DP853F {
         return t[j];
     }
 };
-// stage times c_s (a runtime stage index reads them from the constant bank)
-static __constant__ float kC32[12] = {0.f, F_(DP853_C_2), F_(DP853_C_3), F_(DP853_C_4), F_(DP853_C_5),
-                               F_(DP853_C_6), F_(DP853_C_7), F_(DP853_C_8), F_(DP853_C_9),
-                               F_(DP853_C_10), F_(DP853_C_11), 1.0f};
+// stage times c_s
+__host__ __device__ constexpr float dp853_c32(int s)
+{
+    constexpr float t[12] = {0.f, F_(DP853_C_2), F_(DP853_C_3), F_(DP853_C_4), F_(DP853_C_5),
+                             F_(DP853_C_6), F_(DP853_C_7), F_(DP853_C_8), F_(DP853_C_9),
+                             F_(DP853_C_10), F_(DP853_C_11), 1.0f};
+    return t[s];
+}
 #undef F_
 
 constexpr int kThreads32 = 128;
@@ -142,14 +146,15 @@ __device__ __forceinline__ void stage_terms(const float2* kc, float& x, float& y
     }
 }
 
-// Stage argument combination for a compile-time stage S.
+// Stage argument combination and stage time c_S for a compile-time stage S.
 template <int S, int KS>
-__device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* a1)
+__device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* a1, float* c)
 {
     float x = 0.f, y = 0.f;
     stage_terms<S, KS>(kc, x, y);
     *a0 = x;
     *a1 = y;
+    *c = dp853_c32(S);
 }
 
 // The step's solution increment sum b_j k_j and the two error estimates
@@ -181,21 +186,22 @@ __device__ __forceinline__ void step_sums(const float2* kc, float* b, float* e5,
 // The same for a runtime stage s that is uniform across the warp (one branch
 // of a jump table instead of eleven predicated terms per stage).
 template <int KS>
-__device__ __forceinline__ void stage_combo(int s, const float2* kc, float* a0, float* a1)
+__device__ __forceinline__ void stage_combo(int s, const float2* kc, float* a0, float* a1,
+                                            float* c)
 {
     switch (s) {
-    case 0: *a0 = 0.f; *a1 = 0.f; break;
-    case 1: stage_combo<1, KS>(kc, a0, a1); break;
-    case 2: stage_combo<2, KS>(kc, a0, a1); break;
-    case 3: stage_combo<3, KS>(kc, a0, a1); break;
-    case 4: stage_combo<4, KS>(kc, a0, a1); break;
-    case 5: stage_combo<5, KS>(kc, a0, a1); break;
-    case 6: stage_combo<6, KS>(kc, a0, a1); break;
-    case 7: stage_combo<7, KS>(kc, a0, a1); break;
-    case 8: stage_combo<8, KS>(kc, a0, a1); break;
-    case 9: stage_combo<9, KS>(kc, a0, a1); break;
-    case 10: stage_combo<10, KS>(kc, a0, a1); break;
-    default: stage_combo<11, KS>(kc, a0, a1); break;
+    case 0: *a0 = 0.f; *a1 = 0.f; *c = 0.f; break;
+    case 1: stage_combo<1, KS>(kc, a0, a1, c); break;
+    case 2: stage_combo<2, KS>(kc, a0, a1, c); break;
+    case 3: stage_combo<3, KS>(kc, a0, a1, c); break;
+    case 4: stage_combo<4, KS>(kc, a0, a1, c); break;
+    case 5: stage_combo<5, KS>(kc, a0, a1, c); break;
+    case 6: stage_combo<6, KS>(kc, a0, a1, c); break;
+    case 7: stage_combo<7, KS>(kc, a0, a1, c); break;
+    case 8: stage_combo<8, KS>(kc, a0, a1, c); break;
+    case 9: stage_combo<9, KS>(kc, a0, a1, c); break;
+    case 10: stage_combo<10, KS>(kc, a0, a1, c); break;
+    default: stage_combo<11, KS>(kc, a0, a1, c); break;
     }
 }
 
@@ -274,11 +280,11 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
 #pragma unroll 1
         for (int s = 0; s < 12; ++s) {
             if (s == 0 && !fsal) continue;
-            float a0, a1;
-            stage_combo<KS>(s, kc, &a0, &a1);
+            float a0, a1, cs;
+            stage_combo<KS>(s, kc, &a0, &a1, &cs);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
-            fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);
+            fl(x.hi, fmaf(cs, h, x.lo), yh, ys, kk, P);
             kc[s * KS] = make_float2(kk[0], kk[1]);
         }
         fsal = false;

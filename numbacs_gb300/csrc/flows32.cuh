@@ -130,7 +130,7 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
                                            bool* outside)
 {
     float u = ((vh + vs) - A.a_h) * A.dinv;
-    if (u != u) { *t = u; return 0; }  // NaN propagates
+    // NaN needs no branch: fmaxf picks cell 0 and the offset below is NaN
     const float top = (float)(A.n - 2);
     int i = (int)floorf(fminf(fmaxf(u, 0.0f), top));
     float fi = (float)i;
@@ -213,12 +213,14 @@ __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const flo
     for (int r = 0; r < S::kLevels; ++r) {
         const int a = a0 + r;
         const float wt = bspline_w32_one(ft, a);
-        const float* base = c + 8 * ((size_t)(it + a) * g.st + (size_t)ix * g.sx + iy);
+        // quad-entry index in 32 bits (flows with 2^32 entries or more are refused)
+        const unsigned e0 = (unsigned)(it + a) * (unsigned)g.st + (unsigned)ix * (unsigned)g.sx +
+                            (unsigned)iy;
         float su = 0.0f, sv = 0.0f;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             float p[8];
-            ldg_row8(base + 8 * (size_t)b * g.sx, p);
+            ldg_row8(c + 8 * (size_t)(e0 + (unsigned)b * (unsigned)g.sx), p);
             const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
             const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
             su = fmaf(wx[b], bu, su);
@@ -268,12 +270,13 @@ __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
     for (int rr = 0; rr < S::kLevels; ++rr) {
         const int a = a0 + rr;
         const float wt = bspline_w32_one(ft, a);
-        const float* base = c + 8 * ((size_t)(it + a) * g.st + (size_t)ix * g.sx + iy);
+        const unsigned e0 = (unsigned)(it + a) * (unsigned)g.st + (unsigned)ix * (unsigned)g.sx +
+                            (unsigned)iy;
         float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             float p[8];
-            ldg_row8(base + 8 * (size_t)b * g.sx, p);
+            ldg_row8(c + 8 * (size_t)(e0 + (unsigned)b * (unsigned)g.sx), p);
             const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
             const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
             const float du = fmaf(dwy[0], p[0], fmaf(dwy[1], p[2], fmaf(dwy[2], p[4], dwy[3] * p[6])));
@@ -318,7 +321,7 @@ struct FlowSpline32 {
             //           x % 360               = x - 360 floor(x / 360)             (SPH 2)
             float xv = yh[0] + ys[0];
             float k = floorf((SPH == 1 ? xv + 180.0f : xv) * (1.0f / 360.0f));
-            if (k != 0.0f) xh = fmaf(-360.0f, k, xh);
+            xh = fmaf(-360.0f, k, xh);  // exact no-op for k = 0
         }
         float ft, fx, fy, wx[4], wy[4];
         bool out = false;
@@ -358,7 +361,7 @@ struct FlowSpline32 {
         if (SPH == 1 || SPH == 2) {
             float xv = yh[0] + ys[0];
             float k = floorf((SPH == 1 ? xv + 180.0f : xv) * (1.0f / 360.0f));
-            if (k != 0.0f) xh = fmaf(-360.0f, k, xh);
+            xh = fmaf(-360.0f, k, xh);  // exact no-op for k = 0
         }
         float ft, fx, fy, wx[4], wy[4], dwx[4], dwy[4], r[6];
         bool out = false;

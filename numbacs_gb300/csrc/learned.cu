@@ -158,11 +158,11 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
         yh[1] = y[1].hi;
 #pragma unroll 1
         for (int s = 1; s < 12; ++s) {
-            float a0, a1;
-            stage_combo<kThreads32>(s, kc, &a0, &a1);
+            float a0, a1, cs;
+            stage_combo<kThreads32>(s, kc, &a0, &a1, &cs);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
-            fl(x.hi, fmaf(kC32[s], h, x.lo), yh, ys, kk, P);
+            fl(x.hi, fmaf(cs, h, x.lo), yh, ys, kk, P);
             kc[s * kThreads32] = make_float2(kk[0], kk[1]);
         }
         *nfcn += 11;

@@ -53,6 +53,15 @@ def test_invalid_arguments_are_reported_without_a_gpu():
     rc = L.nbcs_flowmap_grid_2d(f, 0.0, 1.0, None, 1, None, 1, p.ctypes.data_as(_lib._vp), 1,
                                 1e-6, 1e-8, None, None, None, None, None)
     assert rc == -4
+    # the mixed path indexes quad entries in 32 bits: 2^32 spline nodes or more are refused
+    f.extrap = 0
+    f.grid[:] = [0.0, 1.0, 1100.0, 0.0, 1.0, 2000.0, 0.0, 1.0, 2000.0]
+    f.coef_uv, f.coef_uv32 = 4096, 8192  # never dereferenced: validation comes first
+    opts = _lib.NbcsOpts()
+    opts.precision = _lib.PREC_MIXED
+    rc = L.nbcs_flowmap_grid_2d(f, 0.0, 1.0, None, 1, None, 1, p.ctypes.data_as(_lib._vp), 1,
+                                1e-6, 1e-8, None, None, None, opts, None)
+    assert rc == -4 and b"2^32" in L.nbcs_last_error()
     assert L.nbcs_percentile(None, 0, 50.0, None, None, 0, None) == -1
 
 
