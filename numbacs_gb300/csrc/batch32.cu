@@ -14,6 +14,7 @@
 
 #include "batch_common.cuh"
 #include "dop853_32.cuh"
+#include "flowmap_common.cuh"
 
 namespace nbcs {
 

@@ -331,36 +331,4 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
     return status;
 }
 
-// Thread -> (particle group, lane) map for blocks of BT threads.  A block
-// holds BT/LP particles laid out as a (TI x TJ) tile of the grid; tiles run in
-// row-major order.  Inside the tile each warp takes a compact (WI x WJ)
-// sub-tile (4 x 8, 4 x 4, 2 x 4 particles at LP = 1, 2, 4): the fewer spline
-// cells a warp's particles sit in, the more of its stencil gathers hit the
-// same 32-byte entries.  Blocks of two or more warps use tiles TJW wide in y
-// (8 unless given; never narrower than a warp's sub-tile).
-template <int LP, int BT, int TJW = 8>
-struct TileShape {
-    static constexpr int PW = 32 / LP;                   // particles per warp
-    static constexpr int WJ = LP == 1 ? 8 : 4, WI = PW / WJ;
-    static constexpr int PB = BT / LP;                   // particles per block
-    static constexpr int TJ = BT >= 64 && TJW > WJ ? TJW : WJ, TI = PB / TJ;
-    static constexpr int WPJ = TJ / WJ;                  // warps along j
-    static_assert(BT % 32 == 0 && TJ % WJ == 0 && PB % TJ == 0, "tile shape");
-};
-
-template <int LP, int BT = kThreads32, int TJW = 8>
-__device__ __forceinline__ bool tile_particle(long t, int nx, int ny, int* i, int* j)
-{
-    using S = TileShape<LP, BT, TJW>;
-    long tile = t / BT;
-    int r = (int)(t - tile * BT) / LP;
-    int w = r / S::PW, q = r - w * S::PW;
-    int tiles_j = (ny + S::TJ - 1) / S::TJ;
-    long ti = tile / tiles_j;
-    int tj = (int)(tile - ti * tiles_j);
-    *i = (int)(ti * S::TI) + (w / S::WPJ) * S::WI + q / S::WJ;
-    *j = tj * S::TJ + (w % S::WPJ) * S::WJ + q % S::WJ;
-    return *i < nx && *j < ny;
-}
-
 }  // namespace nbcs

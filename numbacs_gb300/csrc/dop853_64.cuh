@@ -63,8 +63,8 @@ struct Dop853Stats {
 };
 
 // Integrate y over solver time [x, xend]; `kc` is this thread's shared-memory
-// column of stage derivatives (stride kThreads64).  Returns NBCS_PARTICLE_*.
-template <class Flow>
+// column of stage derivatives (stride KS, the block size).  Returns NBCS_PARTICLE_*.
+template <class Flow, int KS = kThreads64>
 __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double xend, double* y,
                               double rtol, double atol, int nmax, double2* kc, Dop853Stats* st)
 {
@@ -143,7 +143,7 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
                     if (j < s) {
                         const double c = kA64[s][j];
                         if (c != 0.0) {
-                            const double2 kj = kc[j * kThreads64];
+                            const double2 kj = kc[j * KS];
                             a0 = a0 + c * kj.x;
                             a1 = a1 + c * kj.y;
                         }
@@ -153,14 +153,14 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
                 yy[1] = y[1] + h * a1;
             }
             fl(x + kC64[s] * h, yy, kk, P);
-            kc[s * kThreads64] = make_double2(kk[0], kk[1]);
+            kc[s * KS] = make_double2(kk[0], kk[1]);
         }
         fsal = false;
         st->nfcn += 11;
         double b[2] = {0.0, 0.0}, e5[2] = {0.0, 0.0}, ynew[2];
 #pragma unroll
         for (int j = 0; j < 12; ++j) {
-            const double2 kj = kc[j * kThreads64];
+            const double2 kj = kc[j * KS];
             if (kB64[j] != 0.0) {
                 b[0] = b[0] + kB64[j] * kj.x;
                 b[1] = b[1] + kB64[j] * kj.y;
@@ -170,7 +170,7 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
                 e5[1] = e5[1] + kE5_64[j] * kj.y;
             }
         }
-        const double2 k1 = kc[0], k9 = kc[8 * kThreads64], k12 = kc[11 * kThreads64];
+        const double2 k1 = kc[0], k9 = kc[8 * KS], k12 = kc[11 * KS];
         const double k1v[2] = {k1.x, k1.y}, k9v[2] = {k9.x, k9.y}, k12v[2] = {k12.x, k12.y};
         err = 0.0;
         err2 = 0.0;

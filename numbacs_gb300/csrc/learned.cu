@@ -261,7 +261,7 @@ learned_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restric
          t += (long)gridDim.x * blockDim.x) {
         constexpr int LP = Flow::LP;  // lanes of a group hold the same particle
         int i, j;
-        const bool valid = tile_particle<LP>(t, nx, ny, &i, &j);
+        const bool valid = tile_particle<LP, kThreads32>(t, nx, ny, &i, &j);
         const bool lead = (threadIdx.x & (LP - 1)) == 0;
         const long k = valid ? (long)i * ny + j : 0;
         const bool live = valid && !(mask && mask[k]);
