@@ -102,8 +102,18 @@ static ParamsF to_float(const Params& P)
 }
 
 template <int SPH, class F>
-static int dispatch_lp(int lp, const SplineGridF& g, const float* c, float k, const F& f)
+static int dispatch_lp(int lp, const SplineGridF& g, const float* c, float k, bool exact,
+                       const F& f)
 {
+    // grids whose nodes are floats on every axis (dyadic spacings) take the
+    // cell search without compensated node sums: -3 % on the geophysical flow
+    if (exact) {
+        switch (lp) {
+        case 1: return f(FlowSpline32<SPH, 1, true>{g, c, k});
+        case 2: return f(FlowSpline32<SPH, 2, true>{g, c, k});
+        default: return f(FlowSpline32<SPH, 4, true>{g, c, k});
+        }
+    }
     switch (lp) {
     case 1: return f(FlowSpline32<SPH, 1>{g, c, k});
     case 2: return f(FlowSpline32<SPH, 2>{g, c, k});
@@ -131,10 +141,11 @@ static int dispatch32(const nbcs_flow* flow, int lp, const F& f)
         SplineGridF g = make_grid_f(flow->grid);
         const float* c = flow->coef_uv32;
         float k = (float)(180.0 / (3.141592653589793 * flow->r));
+        const bool ex = grid_nodes_exact_f(flow->grid);
         switch (flow->spherical) {
-        case 1: return dispatch_lp<1>(lp, g, c, k, f);
-        case 2: return dispatch_lp<2>(lp, g, c, k, f);
-        default: return dispatch_lp<0>(lp, g, c, k, f);
+        case 1: return dispatch_lp<1>(lp, g, c, k, ex, f);
+        case 2: return dispatch_lp<2>(lp, g, c, k, ex, f);
+        default: return dispatch_lp<0>(lp, g, c, k, ex, f);
         }
     }
     }

@@ -118,6 +118,26 @@ inline SplineGridF make_grid_f(const double* g)
     return s;
 }
 
+// True when every node a + k d of every axis of the grid tuple g (t0, t1, nt,
+// x0, x1, nx, y0, y1, ny) is a float that fmaf(k, d_h, a_h) reproduces
+// exactly -- dyadic spacings such as 3 h, 0.625 deg, 0.5 deg, 0.25 deg.  The
+// check runs the device formula in double (exact there for these magnitudes).
+inline bool grid_nodes_exact_f(const double* g)
+{
+    for (int d = 0; d < 3; ++d) {
+        double a = g[3 * d], b = g[3 * d + 1];
+        int n = (int)g[3 * d + 2];
+        double dd = (b - a) / (double)(n - 1);
+        float a_h = (float)a, d_h = (float)dd;
+        if ((double)a_h != a || (double)d_h != dd) return false;
+        for (int k = 0; k < n; ++k) {
+            double v = (double)a_h + (double)k * (double)d_h;
+            if ((double)(float)v != v || v != a + (double)k * dd) return false;
+        }
+    }
+    return true;
+}
+
 // Cell index and offset t of the coordinate vh + vs on one axis.  The cell is
 // picked from the rounded coordinate, the offset is formed from the pair
 // (so t may sit a rounding error outside [0, 1] next to a knot, where the two
@@ -126,6 +146,10 @@ inline SplineGridF make_grid_f(const double* g)
 // the ends as pairs -- the hi parts cancel exactly next to an end -- so its
 // sign is the FP64 path's: a particle grid that overshoots the box by 1e-12
 // (np.arange end points) starts outside on both paths.
+// EXACT: the axis nodes are floats and fmaf(k, d_h, a_h) gives them exactly
+// (AxisF::exact, checked on the host); the node position then needs no
+// compensated sum, and the result is the same.
+template <bool EXACT = false>
 __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, float* t,
                                            bool* outside)
 {
@@ -134,14 +158,20 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
     const float top = (float)(A.n - 2);
     int i = (int)floorf(fminf(fmaxf(u, 0.0f), top));
     float fi = (float)i;
-    // node position a + i*d as s + lo (exact product, two-sum on the hi parts)
-    float p = __fmul_rn(fi, A.d_h);
-    float e = fmaf(fi, A.d_h, -p);
-    e = fmaf(fi, A.d_l, e);
-    float s = __fadd_rn(A.a_h, p);
-    float bb = __fsub_rn(s, A.a_h);
-    float err = __fadd_rn(__fsub_rn(A.a_h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    float lo = err + (e + A.a_l);
+    float s, lo;
+    if (EXACT) {  // the node is a float: one FMA (same result as the sum below)
+        s = fmaf(fi, A.d_h, A.a_h);
+        lo = 0.0f;
+    } else {
+        // node position a + i*d as s + lo (exact product, two-sum on the hi parts)
+        float p = __fmul_rn(fi, A.d_h);
+        float e = fmaf(fi, A.d_h, -p);
+        e = fmaf(fi, A.d_l, e);
+        s = __fadd_rn(A.a_h, p);
+        float bb = __fsub_rn(s, A.a_h);
+        float err = __fadd_rn(__fsub_rn(A.a_h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        lo = err + (e + A.a_l);
+    }
     float r = __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
     *t = r * A.dinv;
     if (i == 0) {
@@ -303,7 +333,9 @@ __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
     for (int k = 0; k < 6; ++k) r[k] = acc[k];
 }
 
-template <int SPH, int LP_>
+// EXACT: all three axes have float nodes (AxisF::exact): the cell search skips
+// the compensated node sums (same results).
+template <int SPH, int LP_, bool EXACT = false>
 struct FlowSpline32 {
     static constexpr int LP = LP_;
     SplineGridF g;
@@ -325,9 +357,9 @@ struct FlowSpline32 {
         }
         float ft, fx, fy, wx[4], wy[4];
         bool out = false;
-        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft, &out);
-        int ix = locate_pair(g.ax[1], xh, ys[0], &fx, &out);
-        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy, &out);
+        int it = locate_pair<EXACT>(g.ax[0], p0 * th, p0 * ts, &ft, &out);
+        int ix = locate_pair<EXACT>(g.ax[1], xh, ys[0], &fx, &out);
+        int iy = locate_pair<EXACT>(g.ax[2], yh[1], ys[1], &fy, &out);
         if (out) {  // the lanes of a group agree: they hold the same particle
             dy[0] = 0.0f;
             dy[1] = 0.0f;
@@ -365,9 +397,9 @@ struct FlowSpline32 {
         }
         float ft, fx, fy, wx[4], wy[4], dwx[4], dwy[4], r[6];
         bool out = false;
-        int it = locate_pair(g.ax[0], p0 * th, p0 * ts, &ft, &out);
-        int ix = locate_pair(g.ax[1], xh, ys[0], &fx, &out);
-        int iy = locate_pair(g.ax[2], yh[1], ys[1], &fy, &out);
+        int it = locate_pair<EXACT>(g.ax[0], p0 * th, p0 * ts, &ft, &out);
+        int ix = locate_pair<EXACT>(g.ax[1], xh, ys[0], &fx, &out);
+        int iy = locate_pair<EXACT>(g.ax[2], yh[1], ys[1], &fy, &out);
         if (out) {
             dy[0] = dy[1] = 0.0f;
             J[0] = J[1] = J[2] = J[3] = 0.0f;
