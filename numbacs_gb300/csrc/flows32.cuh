@@ -193,20 +193,6 @@ __device__ __forceinline__ void bspline_w32(float t, float* w)
     w[3] = s * t2 * t;
 }
 
-// B-spline weight of time level a in {0..3} at offset t (one basis function),
-// branch-free: the lanes of a group take different levels, and a switch on a
-// lane-dependent index would serialise the cases.  6 w_a(t) = c3 t^3 + c2 t^2 +
-// c1 t + c0 with (c3, c2, c1, c0) = (-1, 3, -3, 1), (3, -6, 0, 4), (-3, 3, 3, 1),
-// (1, 0, 0, 0).
-__device__ __forceinline__ float bspline_w32_one(float t, int a)
-{
-    const float c3 = a == 0 ? -1.0f : a == 1 ? 3.0f : a == 2 ? -3.0f : 1.0f;
-    const float c2 = a == 0 ? 3.0f : a == 1 ? -6.0f : a == 2 ? 3.0f : 0.0f;
-    const float c1 = a == 0 ? -3.0f : a == 2 ? 3.0f : 0.0f;
-    const float c0 = a == 0 ? 1.0f : a == 1 ? 4.0f : a == 2 ? 1.0f : 0.0f;
-    return (1.0f / 6.0f) * fmaf(fmaf(fmaf(c3, t, c2), t, c1), t, c0);
-}
-
 // Group-cooperative tricubic evaluation.  Coefficients use the "quad" layout:
 // entry k (32 bytes, 32-byte aligned) holds (u_j, v_j) for j = k .. k+3, so the
 // 4 y taps of a stencil row are ONE 256-bit load (ld.global.nc.v8.f32).  The
@@ -219,6 +205,14 @@ template <int LP>
 struct SplineSplit {
     static constexpr int kLevels = 4 / LP;  // time levels per lane
     __device__ static int first_level(int q) { return q * kLevels; }
+    // weight of this lane's r-th level from the four time weights w (selects
+    // on the lane index, no lane-dependent polynomial coefficients)
+    __device__ static float level_weight(const float* w, int q, int r)
+    {
+        if (LP == 1) return w[r];
+        if (LP == 2) return q ? w[2 + r] : w[r];
+        return q == 0 ? w[0] : q == 1 ? w[1] : q == 2 ? w[2] : w[3];
+    }
 };
 
 // one stencil row: taps iy .. iy+3 of (u, v) from a quad entry
@@ -238,11 +232,13 @@ __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const flo
     using S = SplineSplit<LP>;
     const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
     const int a0 = S::first_level(q);  // first time level
+    float wt4[4];
+    bspline_w32(ft, wt4);
     float au = 0.0f, av = 0.0f;
 #pragma unroll
     for (int r = 0; r < S::kLevels; ++r) {
         const int a = a0 + r;
-        const float wt = bspline_w32_one(ft, a);
+        const float wt = S::level_weight(wt4, q, r);
         // quad-entry index in 32 bits (flows with 2^32 entries or more are refused)
         const unsigned e0 = (unsigned)(it + a) * (unsigned)g.st + (unsigned)ix * (unsigned)g.sx +
                             (unsigned)iy;
@@ -295,11 +291,13 @@ __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
     using S = SplineSplit<LP>;
     const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
     const int a0 = S::first_level(q);
+    float wt4[4];
+    bspline_w32(ft, wt4);
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int rr = 0; rr < S::kLevels; ++rr) {
         const int a = a0 + rr;
-        const float wt = bspline_w32_one(ft, a);
+        const float wt = S::level_weight(wt4, q, rr);
         const unsigned e0 = (unsigned)(it + a) * (unsigned)g.st + (unsigned)ix * (unsigned)g.sx +
                             (unsigned)iy;
         float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
