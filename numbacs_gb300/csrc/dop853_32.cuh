@@ -298,7 +298,8 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
             ynew[i] = f2_axpy(y[i], h, b[i]);
             float yo = y[i].hi + y[i].lo, yn = ynew[i].hi + ynew[i].lo;
             float sk = fmaf(rtol, fmaxf(fabsf(yo), fabsf(yn)), atol);
-            float q3 = e3[i] / sk, q5 = e5[i] / sk;
+            const float rs = __frcp_rn(sk);
+            float q3 = e3[i] * rs, q5 = e5[i] * rs;
             err2 = fmaf(q3, q3, err2);
             err = fmaf(q5, q5, err);
         }
@@ -306,8 +307,10 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
         if (deno <= 0.f) deno = 1.f;
         err = fabsf(h) * err * rsqrtf(deno * 2.0f);
         if (isnan(err)) { status = NBCS_PARTICLE_NONFINITE; break; }
-        float fac11 = nbcs_root8f(err);  // err^(1/8)
-        float fac = fmaxf(facc2, fminf(facc1, fac11 / safe));
+        // err^(1/8) and the error ratios to a few ulp: step-size control needs
+        // no more, and the IEEE divisions and square roots cost issue slots
+        float fac11 = exp2f(0.125f * __log2f(err));  // err^(1/8)
+        float fac = fmaxf(facc2, fminf(facc1, fac11 * (1.0f / safe)));
         float hnew = h / fac;
         if (err <= 1.0f) {
             ++*acc;
@@ -321,7 +324,7 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
             if (reject) hnew = posneg * fminf(fabsf(hnew), fabsf(h));
             reject = false;
         } else {
-            hnew = h / fminf(facc1, fac11 / safe);
+            hnew = h / fminf(facc1, fac11 * (1.0f / safe));
             reject = true;
             if (*acc >= 1) ++*rej;
             last = false;

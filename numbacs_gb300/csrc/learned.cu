@@ -175,7 +175,8 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             ynew[i] = f2_axpy(y[i], h, b[i]);
             float yo = y[i].hi + y[i].lo, yn = ynew[i].hi + ynew[i].lo;
             float sk = fmaf(rtol, fmaxf(fabsf(yo), fabsf(yn)), atol);
-            float q3 = e3[i] / sk, q5 = e5[i] / sk;
+            const float rs = __frcp_rn(sk);
+            float q3 = e3[i] * rs, q5 = e5[i] * rs;
             err2 = fmaf(q3, q3, err2);
             err = fmaf(q5, q5, err);
         }
@@ -187,8 +188,8 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             active = false;
             continue;
         }
-        const float fac11 = nbcs_root8f(err);
-        const float fac = fmaxf(facc2, fminf(facc1, fac11 / safe));
+        const float fac11 = exp2f(0.125f * __log2f(err));  // err^(1/8)
+        const float fac = fmaxf(facc2, fminf(facc1, fac11 * (1.0f / safe)));
         float hnew = h / fac;
         if (err <= 1.0f) {
             ++*acc;
@@ -226,7 +227,7 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             if (reject) hnew = posneg * fminf(fabsf(hnew), fabsf(h));
             reject = false;
         } else {
-            hnew = h / fminf(facc1, fac11 / safe);
+            hnew = h / fminf(facc1, fac11 * (1.0f / safe));
             reject = true;
             if (*acc >= 1) ++*rej;
             last = false;
