@@ -43,8 +43,12 @@ flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restr
                  float atol, int nmax, long nthreads)
 {
     constexpr int LP = Flow::LP;
-    __shared__ float2 ks[12 * kFm32Block];
-    float2* kc = ks + threadIdx.x;
+    // the LP lanes of a particle compute identical stage derivatives (the
+    // split RHS ends in a butterfly sum): one shared column per particle, read
+    // as a broadcast by its lanes
+    constexpr int KS = kFm32Block / LP;
+    __shared__ float2 ks[12 * KS];
+    float2* kc = ks + threadIdx.x / LP;
     const F2 xs = f2_from_double(ts), xe = f2_from_double(te);
     // every lane of a group walks the same trip count (nthreads is a multiple of kFm32Block)
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nthreads;
@@ -56,8 +60,7 @@ flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restr
         int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
         if (particle_start(aux, x, y, mask, nx, i, j, &x0, &y0)) {
             F2 yv[2] = {f2_from_double(x0), f2_from_double(y0)};
-            st = dop853_solve32<Flow, kFm32Block>(fl, P, xs, xe, yv, rtol, atol, nmax, kc, &a,
-                                                  &rj, &nf);
+            st = dop853_solve32<Flow, KS>(fl, P, xs, xe, yv, rtol, atol, nmax, kc, &a, &rj, &nf);
             r0 = f2_to_double(yv[0]);
             r1 = f2_to_double(yv[1]);
         }
