@@ -250,3 +250,25 @@ def test_flowmap_all_masked(nb):
                                     return_status=True)
         assert np.array_equal(fm, np.zeros((12, 6, 2)))
         assert (st == st.flat[0]).all() and st.flat[0] != 0
+
+
+def test_mixed_precision_non_dyadic_grid(nb):
+    """A spline grid whose nodes are not floats (0.9 deg and 50/83 deg
+    spacings): the mixed path takes the compensated cell search and stays as
+    close to a tight FP64 solve as the FP64 path at the same rtol."""
+    from numbacs_gb300 import workloads as W
+    t = np.arange(41) * 3.0
+    lon, lat = np.linspace(-100.0, 35.0, 151), np.linspace(-5.0, 45.0, 84)
+    _, _, _, U, V = W.geo_velocity(0, t=t, lon=lon, lat=lat, nmodes=64)
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, U, V)
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    xf, yf = np.linspace(-90.0, 25.0, 61), np.linspace(0.0, 40.0, 31)
+    p = np.array([-1.0])
+    truth = nb.flowmap_grid_2D(fl, 100.0, -48.0, xf, yf, p, rtol=1e-12, atol=1e-14)
+    plain = nb.flowmap_grid_2D(fl, 100.0, -48.0, xf, yf, p, rtol=1e-7, atol=1e-9)
+    mixed, st = nb.flowmap_grid_2D(fl, 100.0, -48.0, xf, yf, p, rtol=1e-7, atol=1e-9,
+                                   precision="mixed", return_status=True)
+    assert (st == 0).all()
+    ep, em = _err_stats(plain, truth), _err_stats(mixed, truth)
+    assert em["median"] <= 3 * ep["median"] + 1e-9, (em, ep)
+    assert em["q99"] <= 3 * ep["q99"] + 1e-8, (em, ep)
