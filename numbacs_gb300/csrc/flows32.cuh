@@ -120,8 +120,11 @@ inline SplineGridF make_grid_f(const double* g)
 
 // True when every node a + k d of every axis of the grid tuple g (t0, t1, nt,
 // x0, x1, nx, y0, y1, ny) is a float that fmaf(k, d_h, a_h) reproduces
-// exactly -- dyadic spacings such as 3 h, 0.625 deg, 0.5 deg, 0.25 deg.  The
-// check runs the device formula in double (exact there for these magnitudes).
+// exactly, and so is every product k d_h -- dyadic spacings such as 3 h,
+// 0.625 deg, 0.5 deg, 0.25 deg.  Then the compensated node sum of
+// locate_pair has zero error terms and the one-FMA form gives the same bits.
+// The check runs the device formulas in double (exact there for these
+// magnitudes).
 inline bool grid_nodes_exact_f(const double* g)
 {
     for (int d = 0; d < 3; ++d) {
@@ -131,8 +134,10 @@ inline bool grid_nodes_exact_f(const double* g)
         float a_h = (float)a, d_h = (float)dd;
         if ((double)a_h != a || (double)d_h != dd) return false;
         for (int k = 0; k < n; ++k) {
-            double v = (double)a_h + (double)k * (double)d_h;
-            if ((double)(float)v != v || v != a + (double)k * dd) return false;
+            double pk = (double)k * (double)d_h;
+            double v = (double)a_h + pk;
+            if ((double)(float)pk != pk || (double)(float)v != v || v != a + (double)k * dd)
+                return false;
         }
     }
     return true;
