@@ -32,6 +32,11 @@ def _fields(nb):
         Field(bj, 0.0, 5.0, np.linspace(0, dom[0][1], 33), np.linspace(-3, 3, 17), pbj, ftle=False),
         Field(dg, 0.0, 8.0, np.linspace(0, 2, 3), np.linspace(0, 1, 3), pdg * np.array([-1, 1, 1, 1, 1, 1])),
     ]
+    # a masked spline field (checkerboard, as the reference's tests mask grids)
+    m = np.zeros((23, 17), bool)
+    m[::2, ::2] = True
+    fs.append(Field(geo, 175.0, -40.0, np.linspace(lon[1], lon[-2], 23),
+                    np.linspace(lat[1], lat[-2], 17), np.array([-1.0]), mask=m))
     return fs
 
 
@@ -49,12 +54,12 @@ def test_batch_equals_single_field(nb, precision, graph, schedule):
         # the batch runs spline fields of the mixed path two lanes per particle
         lp = 2 if (precision == "mixed" and f.flow.kind == 2) else 1
         ref, st = nb.flowmap_grid_2D(f.flow, f.t0, f.T, f.x, f.y, f.params, rtol=f.rtol,
-                                     atol=f.atol, precision=precision, return_status=True,
-                                     lanes_per_particle=lp)
+                                     atol=f.atol, mask=f.mask, precision=precision,
+                                     return_status=True, lanes_per_particle=lp)
         assert torch.equal(f.status, st)
         assert torch.equal(f.flowmap, ref), (precision, float((f.flowmap - ref).abs().max()))
         if f.ftle is not None:
-            ft, ev = nb.ftle_evec_2D(ref, f.T, f.dx, f.dy)
+            ft, ev = nb.ftle_evec_2D(ref, f.T, f.dx, f.dy, mask=f.mask)
             assert torch.equal(f.ftle, ft) and torch.equal(f.evec, ev)
 
 
