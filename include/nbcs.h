@@ -261,6 +261,24 @@ int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, const double* x
                         double f_min, uint8_t* mask_out, double* rpts_full, double* pts_out,
                         int64_t* n_out, void* scratch, size_t scratch_bytes, void* stream);
 
+/* ftle_ordered_ridges (ridges.py:720-1054), host side: link the ridge points
+ * of a ridge test (ridge_mask (nx, ny) u8 and r_pts (nx*ny, 2) as
+ * nbcs_ridge_pts writes them, copied to the host) into curves, strongest
+ * ridge first, and join curves whose endpoints lie within dist_tol with
+ * tangents within ep_tan_ang; drops ridges shorter than min_ridge_pts as the
+ * reference does.  All arrays are HOST memory (f (nx, ny), evec_max (nx, ny,
+ * 2), x, y).  Output: the points of every ridge, one after another, in
+ * pts_out (max_pts x 2) and each ridge's point count in ridge_len_out
+ * (max_ridges); *n_pts, *n_ridges receive the totals (also when the buffers
+ * are too small, which returns NBCS_ERR_SCRATCH).  Every ridge point belongs
+ * to at most one ridge, so max_pts = max_ridges = number of mask points
+ * always suffices. */
+int nbcs_order_ridges(const double* f, const double* evec_max, const double* x, int32_t nx,
+                      const double* y, int32_t ny, const uint8_t* ridge_mask, const double* r_pts,
+                      double dist_tol, double ep_tan_ang, int64_t min_ridge_pts, double sdd_thresh,
+                      double c, double* pts_out, int64_t max_pts, int64_t* ridge_len_out,
+                      int64_t max_ridges, int64_t* n_pts, int64_t* n_ridges);
+
 /* 8-connected component labels of a mask (nx, ny) u8 -> labels (nx, ny)
  * int32: 0 background, 1..n numbered by each component's first pixel in
  * row-major order, exactly as scipy.ndimage.label with a 3x3 structure

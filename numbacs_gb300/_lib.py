@@ -81,6 +81,8 @@ SIGNATURES = {
     "nbcs_ridge_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_ridge_pts": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp, _vp, _vp,
                                       _vp, _sz, _vp]),
+    "nbcs_order_ridges": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp, _d, _d, _i64,
+                                         _d, _d, _vp, _i64, _vp, _i64, _vp, _vp]),
     "nbcs_label8_scratch_bytes": (_sz, [_i32, _i32]),
     "nbcs_label8": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp, _sz, _vp]),
     "nbcs_mlp_blob_bytes": (_sz, []),

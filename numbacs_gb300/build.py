@@ -40,6 +40,7 @@ SOURCES = [
     ("learned.cu", []),
     ("label.cu", []),
     ("compose.cu", ["-fmad=false"]),
+    ("ordered.cu", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

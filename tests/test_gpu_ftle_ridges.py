@@ -233,9 +233,9 @@ def test_ordered_ridges_golden(nb, golden, coords_dg):
 
 @pytest.mark.parametrize("pct", [0, 80])
 def test_ordered_ridges_match_oracle_fed(nb, orc, pct):
-    """A larger field: the GPU-fed ordered ridges equal the oracle-fed ones
-    (same host linking, bit-identical ridge tests)."""
-    from numbacs_gb300.extraction.ordered import ordered_from_ridge_field
+    """A larger field: the GPU ridge test + native linking equal the oracle's
+    ridge test + the oracle's restatement of the linking."""
+    from oracle.ordered_ref import ordered_from_ridge_field
     nx, ny = 301, 157
     x, y, fm = _ridge_field(nx, ny, seed=5)
     dx, dy = x[1] - x[0], y[1] - y[0]

@@ -219,10 +219,22 @@ def test_C_eig_aux_2D(orc, golden, mask_dg):
     assert (ev4[1:-1, 1:-1, 1] > 0).all()
 
 
-def test_ordered_ridges_golden(orc, golden, coords_dg):
-    """tests/test_extraction.py:22-28: the host-side linking of
-    numbacs_gb300.extraction.ordered fed by the oracle's ridge test."""
+def _native_ordered():
+    from numbacs_gb300 import build
+    build.build()
     from numbacs_gb300.extraction.ordered import ordered_from_ridge_field
+    return ordered_from_ridge_field
+
+
+@pytest.mark.parametrize("impl", ["oracle", "native"])
+def test_ordered_ridges_golden(orc, golden, coords_dg, impl):
+    """tests/test_extraction.py:22-28: the linking of the oracle restatement
+    and of the native nbcs_order_ridges (host code), fed by the oracle's ridge
+    test."""
+    if impl == "oracle":
+        from oracle.ordered_ref import ordered_from_ridge_field
+    else:
+        ordered_from_ridge_field = _native_ordered()
     x, y = coords_dg
     f = golden["ftle"].astype(np.float64)
     e = np.ascontiguousarray(golden["Cevecs"][:, :, :, 1].astype(np.float64))
@@ -235,10 +247,40 @@ def test_ordered_ridges_golden(orc, golden, coords_dg):
         assert np.allclose(ridges[k], golden["ordered_%d" % k])
 
 
+def _ridge_test_field(orc, nx, ny, seed):
+    rng = np.random.default_rng(seed)
+    x, y = np.linspace(0, 2, nx), np.linspace(0, 1, ny)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    fm = np.stack([X + 0.05 * np.sin(7 * Y + 3 * X) + 0.03 * np.sin(23 * X * Y),
+                   Y + 0.05 * np.cos(5 * X) + 0.02 * np.cos(17 * Y - 4 * X)], -1)
+    fm = fm + 1e-3 * rng.standard_normal(fm.shape)
+    ev, vec = orc.C_eig_2D(fm, x[1] - x[0], y[1] - y[0])
+    f = orc.ftle_from_eig(ev[..., 1], 5.0)
+    return x, y, f, np.ascontiguousarray(vec[..., :, 1])
+
+
+@pytest.mark.parametrize("nx,ny,seed,pct,tol", [(301, 157, 0, 0, 0.02), (676, 251, 1, 90, 0.05),
+                                                (400, 400, 2, 50, 0.01), (120, 90, 3, 0, 0.2)])
+def test_ordered_ridges_native_equals_oracle(orc, nx, ny, seed, pct, tol):
+    """The native linker makes the restatement's decisions: the same curves,
+    point for point, on fields with thousands of ridge points."""
+    from oracle.ordered_ref import ordered_from_ridge_field as ref
+    native = _native_ordered()
+    x, y, f, e = _ridge_test_field(orc, nx, ny, seed)
+    rpts, mask, _ = orc.ridge_field(f, e, x, y, 0.0, pct)
+    assert mask.sum() > 100
+    for kw in ({}, {"min_ridge_pts": 2, "ep_tan_ang": 0.3}, {"c": 0.0}):
+        a = ref(f, e, x, y, mask, rpts, tol, **kw)
+        b = native(f, e, x, y, mask, rpts, tol, **kw)
+        assert len(a) == len(b) and len(a) > 0
+        for ra, rb in zip(a, b):
+            assert np.array_equal(ra, rb)
+
+
 def test_ordered_ridges_options(orc, golden, coords_dg):
     """min_ridge_pts and the endpoint tolerances act as filters: fewer or equal
     curves, every curve one of the ridge points' paths."""
-    from numbacs_gb300.extraction.ordered import ordered_from_ridge_field
+    ordered_from_ridge_field = _native_ordered()
     x, y = coords_dg
     f = golden["ftle"].astype(np.float64)
     e = np.ascontiguousarray(golden["Cevecs"][:, :, :, 1].astype(np.float64))
