@@ -431,7 +431,7 @@ def run_ours(args, rank, world):
     if not args.quick and not args.no_batch:
         out["batch"] = run_batch(wl, rtol, max(2, min(args.steps, 5)))
     if not args.quick and not args.no_rows:
-        out["composition"], out["aux_grid"] = run_rows(wl, rtol)
+        out["composition"], out["aux_grid"], out["ordered_ridges"] = run_rows(wl, rtol)
     if not args.no_e2e and not args.quick:
         out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
     if not args.no_cpu_baseline and not args.quick and rank == 0:
@@ -706,7 +706,8 @@ def _hbm_peak():
 
 
 def run_rows(wl, rtol, nT=72):
-    """Flow-map composition and the auxiliary grid on the headline workload.
+    """Flow-map composition, the auxiliary grid and ordered ridges on the
+    headline workload.
 
     Composition: nT = 72 one-hour maps of the 676 x 251 particle grid (mixed
     path, t0 = 180 h, backward), composed into the 72 h map; one composition
@@ -764,7 +765,20 @@ def run_rows(wl, rtol, nT=72):
     aux = {"grid": [nx, ny], "precision": "fp64", "rtol": rtol, "h": 1e-5,
            "particles": n_aux, "ms": ms_aux, "particles_per_s": n_aux / (ms_aux * 1e-3),
            "c_eig_aux_ms": a.elapsed_time(b)}
-    return comp, aux
+    # ordered ridges of the 72 h FTLE field (GPU ridge test + native host
+    # linking), host wall clock per call including the copies to the host
+    f, e = nb.ftle_evec_2D(nb.flowmap_composition(fms, grid, nT), wl["T"], wl["dx"], wl["dy"])
+    nb.ftle_ordered_ridges(f, e, x, y, 0.5, percentile=wl["pct"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        ridges = nb.ftle_ordered_ridges(f, e, x, y, 0.5, percentile=wl["pct"])
+    ms_ord = (time.perf_counter() - t0) * 1e3 / reps
+    ordered = {"grid": [nx, ny], "percentile": wl["pct"], "dist_tol_deg": 0.5,
+               "ridges": len(ridges), "points": int(sum(len(r) for r in ridges)),
+               "ms_per_call": ms_ord}
+    return comp, aux, ordered
 
 
 def run_e2e(nb, D, wl, prec, rtol, atol, args, world):
