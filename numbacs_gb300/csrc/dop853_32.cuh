@@ -10,8 +10,9 @@
 //
 // Code shape (from the profile of the fully unrolled version, which was
 // instruction-fetch bound): the twelve stages run as one rolled loop so the
-// right-hand side is instantiated once; the stage derivatives live in shared
-// memory (one column per thread) and the tableau in constant memory.
+// right-hand side is instantiated once; the stage derivatives live in a
+// shared-memory column of stride KS (one per thread, or one per particle whose
+// lanes share it) and the tableau is a set of compile-time constants.
 #pragma once
 
 #include "detmath.h"

@@ -10,7 +10,8 @@
 // Code shape (from the profile of the fully unrolled version, which was
 // instruction-fetch bound): the twelve stages run as one rolled loop so the
 // right-hand side is instantiated once; the stage derivatives live in shared
-// memory (one column per thread) and the tableau in constant memory.
+// memory (one column per particle, shared by its lanes) and the tableau is a
+// set of compile-time constants (zero coefficients cost nothing).
 //
 // Work mapping: a group of LP lanes (1, 2 or 4) integrates one particle; the
 // spline RHS splits its 4 time levels over the group.  Particles are taken in
