@@ -293,3 +293,31 @@ def test_ordered_ridges_options(orc, golden, coords_dg):
         ridges = ordered_from_ridge_field(f, e, x, y, mask, rpts, args.pop("dist_tol"), **args)
         for r in ridges:
             assert all(tuple(p) in pts for p in r)
+
+
+def test_ordered_ridges_native_buffers(orc, golden, coords_dg):
+    """nbcs_order_ridges reports the totals and refuses buffers that are too
+    small (host code; no GPU)."""
+    import ctypes
+    from numbacs_gb300 import _lib, build
+    build.build()
+    L = _lib.load()
+    x, y = coords_dg
+    f = np.ascontiguousarray(golden["ftle"].astype(np.float64))
+    e = np.ascontiguousarray(golden["Cevecs"][:, :, :, 1].astype(np.float64))
+    rpts, mask, _ = orc.ridge_field(f, e, x, y)
+    m = np.ascontiguousarray(mask, np.uint8)
+    rp = np.ascontiguousarray(rpts)
+    n_pts, n_r = ctypes.c_int64(0), ctypes.c_int64(0)
+    vp = _lib._vp
+    args = [f.ctypes.data_as(vp), e.ctypes.data_as(vp), x.ctypes.data_as(vp), len(x),
+            y.ctypes.data_as(vp), len(y), m.ctypes.data_as(vp), rp.ctypes.data_as(vp), 0.1,
+            np.pi / 4, 5, 0.0, 1.0]
+    pts = np.empty((1, 2))
+    lens = np.empty(1, np.int64)
+    rc = L.nbcs_order_ridges(*args, pts.ctypes.data_as(vp), 1, lens.ctypes.data_as(vp), 1,
+                             ctypes.byref(n_pts), ctypes.byref(n_r))
+    assert rc == -3 and n_r.value == int(golden["n_ordered"])
+    assert n_pts.value == sum(golden["ordered_%d" % k].shape[0] for k in range(n_r.value))
+    rc = L.nbcs_order_ridges(*args, None, 0, None, 0, None, None)
+    assert rc == -1
