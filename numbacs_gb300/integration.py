@@ -188,18 +188,29 @@ def flowmap_composition(flowmaps, grid, nT, *, first=0):
     return D.finish(out, as_torch)
 
 
-def flowmap_composition_initial(funcptr, t0, T, h, x, y, grid, params, **kwargs):
+def flowmap_composition_initial(funcptr, t0, T, h, x, y, grid, params, *, streams=8,
+                                **kwargs):
     """integration.py:644-685: the nT = |round(T / h)| flow maps over
     [t0 + k h, t0 + (k + 1) h] and their composition -> (flowmap0, flowmaps, nT).
-    ``kwargs`` go to flowmap_grid_2D."""
+    ``kwargs`` go to flowmap_grid_2D.  The nT integrations are independent:
+    they run on ``streams`` parallel streams (forked from and joined back into
+    the current stream), so the tail of one short integration overlaps the
+    next; the maps are the same whatever the stream count."""
     D.require_cuda()
     as_torch = D.is_torch(x, y)
     xd, yd = D.to_dev(x), D.to_dev(y)
     nT = abs(round(T / h))
     fms = D.empty((nT, xd.numel(), yd.numel(), 2))
+    main = torch.cuda.current_stream()
+    pool = [torch.cuda.Stream() for _ in range(max(1, min(int(streams), nT)))]
+    for s in pool:
+        s.wait_stream(main)
     for k in range(nT):
-        flowmap_grid_2D(funcptr, t0, h, xd, yd, params, out=fms[k], **kwargs)
+        with torch.cuda.stream(pool[k % len(pool)]):
+            flowmap_grid_2D(funcptr, t0, h, xd, yd, params, out=fms[k], **kwargs)
         t0 += h
+    for s in pool:
+        main.wait_stream(s)
     fm0 = flowmap_composition(fms, grid, nT)
     return D.finish(fm0, as_torch), D.finish(fms, as_torch), nT
 
