@@ -34,7 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "FTLE particles/s at <=1e-6 flowmap err vs FP64; mixed/learned vs plain, same GPU"
+METRIC = "FTLE particles/s at \u22641e-6 flowmap err vs FP64; mixed/learned vs plain, same GPU"
 UNIT = "particles/s"
 L2_FLUSH_BYTES = 512 << 20  # > 126 MB L2
 RTOL_LADDER = [1e-6, 3e-7, 1e-7, 3e-8, 1e-8]
