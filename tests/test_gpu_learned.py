@@ -64,7 +64,7 @@ def _geo_flow(nb, seed=0):
     return nb.get_flow_2D(grid, Cu, Cv, spherical=1), lon, lat
 
 
-def test_log_steps_and_proposer_keep_accuracy(nb):
+def test_log_steps_and_proposer_keep_accuracy(nb, record_property):
     from numbacs_gb300.learned import StepProposer, log_steps
     fl, lon, lat = _geo_flow(nb, 0)
     xf = np.linspace(lon[0], lon[-1], 65)
@@ -89,3 +89,20 @@ def test_log_steps_and_proposer_keep_accuracy(nb):
         e_pl = np.median(np.abs(plain - truth).max(-1))
         # the error estimate still judges every step: same accuracy class
         assert e_ml <= 5 * e_pl + 1e-7, (mode, e_ml, e_pl)
+        if mode == 1:
+            # what the network gains over the controller alone: min(proposal,
+            # controller) cuts the steps the controller would have had
+            # rejected -- the rejected fraction falls; the RHS evaluations per
+            # particle are recorded beside it (they do not fall on this flow)
+            def rej(s):
+                s = s.astype(np.float64)
+                return s[..., 1].sum() / (s[..., 0] + s[..., 1]).sum()
+            r_pl, r_ml = rej(pst), rej(mst)
+            nf_pl, nf_ml = float(pst[..., 2].mean()), float(mst[..., 2].mean())
+            record_property("rejected_fraction_plain", r_pl)
+            record_property("rejected_fraction_learned", r_ml)
+            record_property("rhs_evals_plain", nf_pl)
+            record_property("rhs_evals_learned", nf_ml)
+            print("learned proposer: rejected %.3f -> %.3f, RHS evals/particle %.1f -> %.1f"
+                  % (r_pl, r_ml, nf_pl, nf_ml))
+            assert r_ml < r_pl, (r_ml, r_pl)
