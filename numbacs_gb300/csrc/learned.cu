@@ -27,12 +27,6 @@
 
 namespace nbcs {
 
-// Threads per block of the proposing integrator: one 16 x 8 particle tile per
-// block (two lanes a particle), as the plain mixed kernel, so that the warps
-// of a block share L1 lines (2.51 ms against 2.89 ms with 8 x 8 tiles of
-// 128 threads, 338 x 126 geophysical particles).
-constexpr int kLearnBlock = 256;
-
 struct LogSink {
     float* feats;
     float* targets;
@@ -165,15 +159,15 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
 #pragma unroll 1
         for (int s = 1; s < 12; ++s) {
             float a0, a1, cs;
-            stage_combo<kLearnBlock>(s, kc, &a0, &a1, &cs);
+            stage_combo<kThreads32>(s, kc, &a0, &a1, &cs);
             ys[0] = fmaf(h, a0, y[0].lo);
             ys[1] = fmaf(h, a1, y[1].lo);
             fl(x.hi, fmaf(cs, h, x.lo), yh, ys, kk, P);
-            kc[s * kLearnBlock] = make_float2(kk[0], kk[1]);
+            kc[s * kThreads32] = make_float2(kk[0], kk[1]);
         }
         *nfcn += 11;
         float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
-        step_sums<kLearnBlock>(kc, b, e5, e3);
+        step_sums<kThreads32>(kc, b, e5, e3);
         F2 ynew[2];
         float err = 0.f, err2 = 0.f;
 #pragma unroll
@@ -243,21 +237,21 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
     *status_out = status;
 }
 
-// Two resident blocks (up to 128 registers a thread, no spills): a tighter cap
-// spills onto the L1 pipe that the spline gathers load (with 128-thread
-// blocks, a 72-register cap measured 36% slower than 96 registers).
+// No register cap: capping at 72 (7 blocks/SM) spills onto the L1 pipe that
+// the spline gathers already saturate and measured 36% slower than the
+// uncapped 96 registers.
 template <class Flow, bool LOG, bool PROPOSE>
-__global__ void __launch_bounds__(kLearnBlock, 2)
+__global__ void __launch_bounds__(kThreads32)
 learned_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restrict__ x,
                const double* __restrict__ y, int nx, int ny, const uint8_t* __restrict__ mask,
                double* __restrict__ out, int32_t* __restrict__ status, int32_t* __restrict__ stats,
                float rtol, float atol, int nmax, long nthreads, const MlpBlob* __restrict__ Wg,
                int mode, LogSink sink)
 {
-    __shared__ float2 ks[12 * kLearnBlock];
+    __shared__ float2 ks[12 * kThreads32];
     __shared__ MlpBlob W;
-    __shared__ __align__(16) __nv_bfloat16 xs[kLearnBlock / 32][32 * kMlpInPad];
-    __shared__ float outs[kLearnBlock / 32][32];
+    __shared__ __align__(16) __nv_bfloat16 xs[kThreads32 / 32][32 * kMlpInPad];
+    __shared__ float outs[kThreads32 / 32][32];
     if (PROPOSE) mlp_stage(Wg, &W);
     __syncthreads();
     float2* kc = ks + threadIdx.x;
@@ -268,7 +262,7 @@ learned_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restric
          t += (long)gridDim.x * blockDim.x) {
         constexpr int LP = Flow::LP;  // lanes of a group hold the same particle
         int i, j;
-        const bool valid = tile_particle<LP, kLearnBlock>(t, nx, ny, &i, &j);
+        const bool valid = tile_particle<LP, kThreads32>(t, nx, ny, &i, &j);
         const bool lead = (threadIdx.x & (LP - 1)) == 0;
         const long k = valid ? (long)i * ny + j : 0;
         const bool live = valid && !(mask && mask[k]);
@@ -309,16 +303,15 @@ static int launch_learned(const nbcs_flow* flow, const FlowmapArgs& a, const Mlp
     const float* c = flow->coef_uv32;
     float kd = (float)(180.0 / (3.141592653589793 * flow->r));
     // two lanes per particle (8 x 8 particle tiles per 128-thread block)
-    constexpr int LPL = 2;
-    using S = TileShape<LPL, kLearnBlock>;
-    long tiles = (long)((a.nx + S::TI - 1) / S::TI) * ((a.ny + S::TJ - 1) / S::TJ);
-    long nthreads = tiles * kLearnBlock;
+    constexpr int LPL = 2, TI = kThreads32 / LPL / 8;
+    long tiles = (long)((a.nx + TI - 1) / TI) * ((a.ny + 7) / 8);
+    long nthreads = tiles * kThreads32;
     long blocks = tiles;
     if (a.blocks_per_sm > 0 && blocks > (long)sm_count() * a.blocks_per_sm)
         blocks = (long)sm_count() * a.blocks_per_sm;
     ParamsF P = to_float_p(a.P);
 #define NBCS_LAUNCH_LEARNED(SPH)                                                              \
-    learned_kernel<FlowSpline32<SPH, LPL>, LOG, PROPOSE><<<(unsigned)blocks, kLearnBlock, 0, a.stream>>>( \
+    learned_kernel<FlowSpline32<SPH, LPL>, LOG, PROPOSE><<<(unsigned)blocks, kThreads32, 0, a.stream>>>( \
         FlowSpline32<SPH, LPL>{g, c, kd}, P, a.ts, a.te, a.x, a.y, a.nx, a.ny, a.mask, a.out,    \
         a.status, a.stats, (float)a.rtol, (float)a.atol, a.nmax, nthreads, W, mode, sink)
     switch (flow->spherical) {
