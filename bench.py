@@ -70,7 +70,8 @@ def parse():
                     help="fixed lanes per particle (with --blocks-per-sm: skips the autotuner)")
     ap.add_argument("--blocks-per-sm", type=int, default=None)
     ap.add_argument("--kernel-case", default=None,
-                    choices=["ftle", "ridge", "compose", "label", "batch", "mlp"],
+                    choices=["ftle", "ridge", "compose", "label", "batch", "mlp", "stencils", "aux",
+                             "prefilter", "learned"],
                     help="run one small case of one kernel family 3 times (for ncu captures)")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no ladder, plain comparison, e2e or CPU baseline)")
@@ -960,7 +961,12 @@ def run_kernel_case(name, reps=3):
     ridge (percentile + ridge points on that FTLE field), compose (72 maps of
     the 676 x 251 grid), label (8-connected labelling of a 4001 x 4001 ridge
     mask), batch (16 geophysical fields at 0.4 deg, tile schedule), mlp (one
-    BF16 gradient pass over 2^20 samples)."""
+    BF16 gradient pass over 2^20 samples), stencils (the unfused ftle_grid_2D
+    and C_eig_2D kernels on the 4001 x 4001 flow map), aux (C_eig_aux_2D on a
+    2001 x 1001 auxiliary-grid flow map, 160 MB), prefilter (the spline
+    prefilter of the geophysical velocity, 121 x 217 x 101), learned (the
+    proposing integrator on the 0.4 deg geophysical grid, network trained on
+    steps logged from that flow)."""
     import torch
     import numbacs_gb300 as nb
     from numbacs_gb300.extraction import ridges as R
@@ -987,6 +993,37 @@ def run_kernel_case(name, reps=3):
                                         Yc + 0.3 * torch.cos(0.1 * Xc + k)], -1)
                            for k in range(nT)]).contiguous()
         fn = lambda: nb.flowmap_composition(fms, ((-100.0, 35.0, nx), (-5.0, 45.0, ny)), nT)  # noqa: E731
+    elif name == "stencils":
+        def fn():
+            nb.ftle_grid_2D(fm, -10.0, dx, dy)
+            nb.C_eig_2D(fm, dx, dy)
+    elif name == "aux":
+        na, nb_ = 2001, 1001
+        Xa, Ya = torch.meshgrid(lin(0, 2, na), lin(0, 1, nb_), indexing="ij")
+        h = 1e-5
+        offs = [(h, 0.0), (-h, 0.0), (0.0, h), (0.0, -h), (0.0, 0.0)]
+        fa = torch.stack([torch.stack([Xa + ox + 0.1 * torch.sin(3 * (Ya + oy)),
+                                       Ya + oy + 0.1 * torch.sin(2 * (Xa + ox))], -1)
+                          for ox, oy in offs], 2).contiguous()
+        fn = lambda: nb.C_eig_aux_2D(fa, 2.0 / (na - 1), 1.0 / (nb_ - 1), h)  # noqa: E731
+    elif name == "prefilter":
+        from numbacs_gb300 import workloads as W
+        t, lon, lat, U, V = W.geo_velocity(seed=0)
+        Ud, Vd = torch.from_numpy(U).cuda(), torch.from_numpy(V).cuda()
+        fn = lambda: nb.get_interp_arrays_2D(t, lon, lat, Ud, Vd)  # noqa: E731
+    elif name == "learned":
+        from numbacs_gb300 import workloads as W
+        from numbacs_gb300.learned import StepProposer, log_steps
+        wl = geo_setup(180.0)
+        lonf, latf = W.geo_ftle_grid(0.4)
+        feats, targ, _ = log_steps(wl["flow"], 180.0, W.GEO_T, lonf, latf, wl["params"],
+                                   rtol=1e-7, atol=1e-9, sample=1.0)
+        sp = StepProposer(seed=0)
+        sp.train(feats, targ, epochs=2)
+        xl, yl = torch.from_numpy(lonf).cuda(), torch.from_numpy(latf).cuda()
+        fn = lambda: nb.flowmap_grid_2D(wl["flow"], 180.0, W.GEO_T, xl, yl, wl["params"],  # noqa: E731
+                                        rtol=1e-7, atol=1e-9, precision="mixed",
+                                        return_status=True, step_model=sp, step_model_mode=1)
     elif name == "batch":
         from numbacs_gb300 import workloads as W
         from numbacs_gb300.batch import Field, FTLEBatch
