@@ -13,10 +13,12 @@
 // block to finish (atomic ticket, no spinning) picks the digit and resets the
 // histogram for the next pass, so no host round trip is needed.
 //
-// Ridge points: pass 1 evaluates the stencil and writes the mask and one
-// count per block of 2048 points; pass 2 scans the counts; pass 3 ranks the
-// flagged points of each block in row-major order (warp ballots) and writes
-// them compacted, re-evaluating the stencil only at flagged points.
+// Ridge points: pass 1 evaluates the stencil and writes the mask (and, when
+// the caller asks for it, the full point array) and one count per block of
+// points; pass 2 scans the counts; pass 3 ranks the flagged points of each
+// block in row-major order (warp ballots) and writes them compacted, gathering
+// them from the full array when there is one, else re-evaluating the stencil
+// at the flagged points only.
 // Compiled with -fmad=false: the stencil arithmetic is the reference's.
 #include <math.h>
 
@@ -424,7 +426,8 @@ ridge_scan_kernel(const unsigned int* __restrict__ cnt, long nb, unsigned long l
 
 __global__ void __launch_bounds__(kRidgeThreads)
 ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
-                     const unsigned long long* __restrict__ off, double2* __restrict__ out)
+                     const unsigned long long* __restrict__ off, const double2* __restrict__ full,
+                     double2* __restrict__ out)
 {
     __shared__ unsigned int wsum[kRidgeThreads / 32];
     const long n = (long)R.nx * R.ny;
@@ -449,7 +452,13 @@ ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
         }
         if (on) {
             double px = 0.0, py = 0.0;
-            ridge_at(R, fmin, dx, dy, k, &px, &py);
+            if (full) {  // the flag pass stored every point: gather it
+                const double2 v = full[k];
+                px = v.x;
+                py = v.y;
+            } else {  // re-evaluate the stencil at the ridge point only
+                ridge_at(R, fmin, dx, dy, k, &px, &py);
+            }
             unsigned int rank = before + __popc(bal & ((1u << lane) - 1u));
             out[run + rank] = make_double2(px, py);
         }
@@ -549,7 +558,7 @@ static int ridge_run(const double* f, const double* evec_max, const double* x, i
     ridge_scan_kernel<<<1, 1024, 0, st>>>(cnt, nb, off, n_out);
     NBCS_LAUNCH_CHECK();
     ridge_compact_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
-        R, mask, off, reinterpret_cast<double2*>(pts_out));
+        R, mask, off, reinterpret_cast<const double2*>(rpts_full), reinterpret_cast<double2*>(pts_out));
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
