@@ -56,7 +56,10 @@ extern "C" {
 typedef struct nbcs_flow {
     int32_t kind;      /* NBCS_FLOW_* */
     int32_t spherical; /* SPLINE2D: 0 planar, 1 lon in [-180,180), 2 lon in [0,360) */
-    int32_t extrap;    /* SPLINE2D: 0 = "constant" (coordinates clamped to the grid box) */
+    int32_t extrap;    /* SPLINE2D, outside the grid box: 0 "constant" (zero velocity),
+                          1 "nearest" (value at the nearest box point), 2 "linear"
+                          (that value plus derivative x distance along each clamped
+                          axis); eval_spline's extrap_mode, flows.py:121 */
     int32_t reserved;
     double r;          /* SPLINE2D spherical: radius (km) for km/h -> deg/h */
     double grid[9];    /* SPLINE2D: t0,t1,nt, x0,x1,nx, y0,y1,ny (UCGrid tuple) */
@@ -339,8 +342,12 @@ int nbcs_flowmap_log_steps(const nbcs_flow* flow, double t0, double T, const dou
  * holds until the process exits.  Grids above NBCS_RIDGE_NOALLOC_MAX_POINTS
  * points are rejected with NBCS_ERR_INVALID.  The first call on a device looks
  * up the array's device address with that device current; make it before any
- * stream capture.  All calls share the array, so calls whose work overlaps on
- * the GPU race on it. */
+ * stream capture.  The address is kept per device ordinal for the life of the
+ * process: it belongs to the device's primary context (the one the CUDA
+ * runtime uses) and is not looked up again after cudaDeviceReset, so do not
+ * call this entry point after resetting the device or from another context
+ * on it.  All calls share the array, so calls whose work overlaps on the GPU
+ * race on it. */
 #define NBCS_RIDGE_NOALLOC_MAX_POINTS (1L << 23)
 size_t nbcs_ridge_noalloc_scratch_bytes(void);
 int nbcs_ridge_pts_noalloc(const double* f, const double* evec_max, const double* x, int32_t nx,

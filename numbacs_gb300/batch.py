@@ -105,12 +105,23 @@ class FTLEBatch:
             s.evec_max = f.evec.data_ptr() if f.evec is not None else None
         self._field_arr = arr
         L = _lib.load()
-        nbytes = L.nbcs_batch_scratch_bytes(len(flows), len(self.fields))
-        self._scratch = torch.empty(nbytes, dtype=torch.uint8, device=D.device())
+        # the batched kernels take spline flows with extrap_mode "constant" only;
+        # a batch holding another mode runs every field through its own launches
+        self.kernels_ok = all(fl.kind != _lib.FLOW_SPLINE2D or fl.extrap == 0 for fl in flows)
         self.plan = _lib.NbcsBatch()
-        _lib.check(L.nbcs_batch_prepare(self._flow_arr, len(flows), self._field_arr,
-                                        len(self.fields), _PREC[precision], D.ptr(self._scratch),
-                                        nbytes, ctypes.byref(self.plan), D.stream_ptr()))
+        self._scratch = None
+        if self.kernels_ok:
+            nbytes = L.nbcs_batch_scratch_bytes(len(flows), len(self.fields))
+            self._scratch = torch.empty(nbytes, dtype=torch.uint8, device=D.device())
+            _lib.check(L.nbcs_batch_prepare(self._flow_arr, len(flows), self._field_arr,
+                                            len(self.fields), _PREC[precision],
+                                            D.ptr(self._scratch), nbytes,
+                                            ctypes.byref(self.plan), D.stream_ptr()))
+        elif blocks_per_sm is not None and int(blocks_per_sm) != STREAMS:
+            raise ValueError("a batch with extrap_mode 'nearest' or 'linear' flows runs only "
+                             "the per-field schedule (blocks_per_sm=%d)" % STREAMS)
+        else:
+            blocks_per_sm = STREAMS
         self.max_steps = int(max_steps)
         self.max_streams = max(1, int(max_streams))
         self._streams = None

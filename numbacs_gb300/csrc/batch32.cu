@@ -174,6 +174,7 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
                                   int32_t nfields, int32_t precision, void* scratch,
                                   size_t scratch_bytes, nbcs_batch* plan, void* stream)
 {
+    NBCS_RANGE();
     if (!flows || !fields || !plan || nflows < 1 || nfields < 1)
         return set_error(NBCS_ERR_INVALID, "batch_prepare: need >= 1 flow and >= 1 field");
     if (precision != NBCS_PREC_FP64 && precision != NBCS_PREC_MIXED)
@@ -207,6 +208,10 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
             return set_error(NBCS_ERR_INVALID, "batch field %d: flow index %d out of range", k, F.flow);
         int rc = validate_flow(&flows[F.flow], F.params, F.np, precision);
         if (rc) return rc;
+        if (flows[F.flow].kind == NBCS_FLOW_SPLINE2D && flows[F.flow].extrap != 0)
+            return set_error(NBCS_ERR_UNSUPPORTED,
+                             "batch field %d: the batched kernels take extrap_mode 'constant' "
+                             "only; run such fields through nbcs_flowmap_grid_2d", k);
         if (F.nx < 0 || F.ny < 0 || ((long)F.nx * F.ny > 0 && (!F.x || !F.y || !F.flowmap)))
             return set_error(NBCS_ERR_INVALID, "batch field %d: bad grid or NULL array", k);
         if (!(F.rtol > 0.0) || !(F.atol > 0.0))
@@ -268,6 +273,7 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
 
 extern "C" int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, void* stream)
 {
+    NBCS_RANGE();
     if (!plan || !plan->scratch) return set_error(NBCS_ERR_INVALID, "batch_run: no plan");
     const BatchLayout lay = batch_layout(plan->nflows, plan->nfields);
     unsigned char* base = static_cast<unsigned char*>(plan->scratch);

@@ -44,13 +44,13 @@ batch64_kernel(BatchHeader* hdr, const DevFlow64* __restrict__ flows,
                 break;
             default:
                 if (fl.spherical == 1)
-                    st = dop853_solve64(FlowSpline64<1>{fl.g, fl.c, fl.r, 0}, F.P, F.ts, F.te, yv,
+                    st = dop853_solve64(FlowSpline64<1>{fl.g, fl.c, fl.r}, F.P, F.ts, F.te, yv,
                                         F.rtol, F.atol, nmax, kc, &s);
                 else if (fl.spherical == 2)
-                    st = dop853_solve64(FlowSpline64<2>{fl.g, fl.c, fl.r, 0}, F.P, F.ts, F.te, yv,
+                    st = dop853_solve64(FlowSpline64<2>{fl.g, fl.c, fl.r}, F.P, F.ts, F.te, yv,
                                         F.rtol, F.atol, nmax, kc, &s);
                 else
-                    st = dop853_solve64(FlowSpline64<0>{fl.g, fl.c, fl.r, 0}, F.P, F.ts, F.te, yv,
+                    st = dop853_solve64(FlowSpline64<0>{fl.g, fl.c, fl.r}, F.P, F.ts, F.te, yv,
                                         F.rtol, F.atol, nmax, kc, &s);
                 break;
             }

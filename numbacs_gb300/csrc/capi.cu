@@ -50,8 +50,10 @@ int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int p
     case NBCS_FLOW_SPLINE2D: {
         if (flow->spherical < 0 || flow->spherical > 2)
             return set_error(NBCS_ERR_INVALID, "spherical must be 0, 1 or 2");
-        if (flow->extrap != 0)
-            return set_error(NBCS_ERR_UNSUPPORTED, "only extrap_mode='constant' is supported");
+        if (flow->extrap < 0 || flow->extrap > 2)
+            return set_error(NBCS_ERR_INVALID,
+                             "extrap must be 0 (constant), 1 (nearest) or 2 (linear), got %d",
+                             flow->extrap);
         for (int d = 0; d < 3; ++d) {
             double n = flow->grid[3 * d + 2];
             if (!(n >= 2.0) || !(flow->grid[3 * d + 1] > flow->grid[3 * d]))

@@ -75,6 +75,7 @@ using namespace nbcs;
 extern "C" int nbcs_flowmap_compose(const double* flowmaps, int32_t nT, int32_t first,
                                     const double* grid, double* out, void* stream)
 {
+    NBCS_RANGE();
     if (!grid) return set_error(NBCS_ERR_INVALID, "compose: NULL grid");
     const double gnx = grid[2], gny = grid[5];
     if (!(gnx >= 2.0 && gny >= 2.0 && gnx <= 2147483647.0 && gny <= 2147483647.0) ||

@@ -106,9 +106,25 @@ static ParamsF to_float(const Params& P)
 }
 
 template <int SPH, class F>
-static int dispatch_lp(int lp, const SplineGridF& g, const float* c, float k, bool exact,
+static int dispatch_lp(int lp, int xm, const SplineGridF& g, const float* c, float k, bool exact,
                        const F& f)
 {
+    // extrapolation beyond the grid box ("nearest", "linear"): the general
+    // cell search only (fewer instantiations; the box test is the same)
+    if (xm == 1) {
+        switch (lp) {
+        case 1: return f(FlowSpline32<SPH, 1, false, 1>{g, c, k});
+        case 2: return f(FlowSpline32<SPH, 2, false, 1>{g, c, k});
+        default: return f(FlowSpline32<SPH, 4, false, 1>{g, c, k});
+        }
+    }
+    if (xm == 2) {
+        switch (lp) {
+        case 1: return f(FlowSpline32<SPH, 1, false, 2>{g, c, k});
+        case 2: return f(FlowSpline32<SPH, 2, false, 2>{g, c, k});
+        default: return f(FlowSpline32<SPH, 4, false, 2>{g, c, k});
+        }
+    }
     // grids whose nodes are floats on every axis (dyadic spacings) take the
     // cell search without compensated node sums: -3 % on the geophysical flow
     if (exact) {
@@ -146,10 +162,11 @@ static int dispatch32(const nbcs_flow* flow, int lp, const F& f)
         const float* c = flow->coef_uv32;
         float k = (float)(180.0 / (3.141592653589793 * flow->r));
         const bool ex = grid_nodes_exact_f(flow->grid);
+        const int xm = flow->extrap;
         switch (flow->spherical) {
-        case 1: return dispatch_lp<1>(lp, g, c, k, ex, f);
-        case 2: return dispatch_lp<2>(lp, g, c, k, ex, f);
-        default: return dispatch_lp<0>(lp, g, c, k, ex, f);
+        case 1: return dispatch_lp<1>(lp, xm, g, c, k, ex, f);
+        case 2: return dispatch_lp<2>(lp, xm, g, c, k, ex, f);
+        default: return dispatch_lp<0>(lp, xm, g, c, k, ex, f);
         }
     }
     }

@@ -113,10 +113,17 @@ static int dispatch64(const nbcs_flow* flow, const F& f)
     default: {
         SplineGrid g = make_grid(flow->grid);
         const double2* c = reinterpret_cast<const double2*>(flow->coef_uv);
-        switch (flow->spherical) {
-        case 1: return f(FlowSpline64<1>{g, c, flow->r, flow->extrap});
-        case 2: return f(FlowSpline64<2>{g, c, flow->r, flow->extrap});
-        default: return f(FlowSpline64<0>{g, c, flow->r, flow->extrap});
+        const double r = flow->r;
+        switch (flow->spherical * 3 + flow->extrap) {  // validate_flow bounds both
+        case 1: return f(FlowSpline64<0, 1>{g, c, r});
+        case 2: return f(FlowSpline64<0, 2>{g, c, r});
+        case 3: return f(FlowSpline64<1, 0>{g, c, r});
+        case 4: return f(FlowSpline64<1, 1>{g, c, r});
+        case 5: return f(FlowSpline64<1, 2>{g, c, r});
+        case 6: return f(FlowSpline64<2, 0>{g, c, r});
+        case 7: return f(FlowSpline64<2, 1>{g, c, r});
+        case 8: return f(FlowSpline64<2, 2>{g, c, r});
+        default: return f(FlowSpline64<0, 0>{g, c, r});
         }
     }
     }
@@ -135,6 +142,7 @@ extern "C" int nbcs_eval_rhs(const nbcs_flow* flow, const double* params, int32_
                              const double* ty, int64_t n, double* dy, int32_t precision,
                              void* stream)
 {
+    NBCS_RANGE();
     int rc = validate_flow(flow, params, np, precision);
     if (rc) return rc;
     if (n < 0 || (n > 0 && (!ty || !dy))) return set_error(NBCS_ERR_INVALID, "eval_rhs: bad arrays");
@@ -157,6 +165,7 @@ extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, 
                                     const uint8_t* mask, double* flowmap, int32_t* status,
                                     const nbcs_opts* opts, void* stream)
 {
+    NBCS_RANGE();
     const AuxGrid plain = {0, ny, 1, 0.0};
     return flowmap_particles(flow, t0, T, x, nx, y, ny, params, np, rtol, atol, mask, flowmap,
                              status, opts, stream, plain);
@@ -169,6 +178,7 @@ extern "C" int nbcs_flowmap_aux_grid_2d(const nbcs_flow* flow, double t0, double
                                         double atol, const uint8_t* mask, double* flowmap_aux,
                                         int32_t* status, const nbcs_opts* opts, void* stream)
 {
+    NBCS_RANGE();
     if (!(h > 0.0) && !(h < 0.0)) return set_error(NBCS_ERR_INVALID, "aux grid: h must be nonzero");
     if (opts && opts->step_model)
         return set_error(NBCS_ERR_UNSUPPORTED, "aux grid: no step_model");

@@ -146,17 +146,19 @@ inline bool grid_nodes_exact_f(const double* g)
 // Cell index and offset t of the coordinate vh + vs on one axis.  The cell is
 // picked from the rounded coordinate, the offset is formed from the pair
 // (so t may sit a rounding error outside [0, 1] next to a knot, where the two
-// cubic pieces agree).  A coordinate strictly outside [a, b] sets *outside
-// (extrap_mode "constant": the interpolant is 0 there).  That test subtracts
-// the ends as pairs -- the hi parts cancel exactly next to an end -- so its
-// sign is the FP64 path's: a particle grid that overshoots the box by 1e-12
-// (np.arange end points) starts outside on both paths.
+// cubic pieces agree).  A coordinate strictly outside [a, b] sets *outside.
+// That test subtracts the ends as pairs -- the hi parts cancel exactly next
+// to an end -- so its sign is the FP64 path's: a particle grid that
+// overshoots the box by 1e-12 (np.arange end points) starts outside on both
+// paths.  With extrapolation mode XM = 1 ("nearest") or 2 ("linear") an
+// outside coordinate is clamped to the box (t = 0 or 1), and for XM = 2 *dl
+// receives its distance beyond the box in cells of this axis.
 // EXACT: the axis nodes are floats and fmaf(k, d_h, a_h) gives them exactly
 // (AxisF::exact, checked on the host); the node position then needs no
 // compensated sum, and the result is the same.
-template <bool EXACT = false>
+template <bool EXACT = false, int XM = 0>
 __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, float* t,
-                                           bool* outside)
+                                           bool* outside, float* dl = nullptr)
 {
     float u = ((vh + vs) - A.a_h) * A.dinv;
     // NaN needs no branch: fmaxf picks cell 0 and the offset below is NaN
@@ -180,9 +182,20 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
     float r = __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
     *t = r * A.dinv;
     if (i == 0) {
-        if (__fadd_rn(__fsub_rn(vh, A.a_h), __fsub_rn(vs, A.a_l)) < 0.0f) *outside = true;
-    } else if (i == A.n - 2) {
-        if (__fadd_rn(__fsub_rn(vh, A.b_h), __fsub_rn(vs, A.b_l)) > 0.0f) *outside = true;
+        const float ex = __fadd_rn(__fsub_rn(vh, A.a_h), __fsub_rn(vs, A.a_l));
+        if (ex < 0.0f) {
+            *outside = true;
+            if (XM != 0) *t = 0.0f;
+            if (XM == 2) *dl = ex * A.dinv;
+        }
+    }
+    if (i == A.n - 2) {  // not "else": on a 2-node axis cell 0 holds both ends
+        const float ex = __fadd_rn(__fsub_rn(vh, A.b_h), __fsub_rn(vs, A.b_l));
+        if (ex > 0.0f) {
+            *outside = true;
+            if (XM != 0) *t = 1.0f;
+            if (XM == 2) *dl = ex * A.dinv;
+        }
     }
     return i;
 }
@@ -336,9 +349,74 @@ __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
     for (int k = 0; k < 6; ++k) r[k] = acc[k];
 }
 
+// Value plus first-order continuation beyond the box (extrapolation "linear"):
+// u + sum_d dl[d] du/d(offset_d) at the clamped point, same for v, with dl in
+// cells of each axis.  Same group split and butterfly as spline_eval_uv32;
+// taken only by particles whose stage point left the grid box.
+template <int LP>
+__device__ __forceinline__ void spline_eval_uv32_lin(const SplineGridF& g, const float* __restrict__ c,
+                                                  int it, int ix, int iy, float ft, float fx,
+                                                  float fy, const float* dl, float* u, float* v)
+{
+    using S = SplineSplit<LP>;
+    const int q = (LP > 1) ? (int)(threadIdx.x & (LP - 1)) : 0;
+    const int a0 = S::first_level(q);
+    float wt4[4], dwt4[4], wx[4], wy[4], dwx[4], dwy[4];
+    bspline_w32(ft, wt4);
+    bspline_dw32(ft, dwt4);
+    bspline_w32(fx, wx);
+    bspline_w32(fy, wy);
+    bspline_dw32(fx, dwx);
+    bspline_dw32(fy, dwy);
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // (u, v) x (value, d/dt, d/dx, d/dy)
+#pragma unroll
+    for (int rr = 0; rr < S::kLevels; ++rr) {
+        const int a = a0 + rr;
+        const float wt = S::level_weight(wt4, q, rr), dwt = S::level_weight(dwt4, q, rr);
+        const unsigned e0 = (unsigned)(it + a) * (unsigned)g.st + (unsigned)ix * (unsigned)g.sx +
+                            (unsigned)iy;
+        float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // (u, v) x (value, d/dx, d/dy) at this level
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            float p[8];
+            ldg_row8(c + 8 * (size_t)(e0 + (unsigned)b * (unsigned)g.sx), p);
+            const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
+            const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
+            const float du = fmaf(dwy[0], p[0], fmaf(dwy[1], p[2], fmaf(dwy[2], p[4], dwy[3] * p[6])));
+            const float dv = fmaf(dwy[0], p[1], fmaf(dwy[1], p[3], fmaf(dwy[2], p[5], dwy[3] * p[7])));
+            s[0] = fmaf(wx[b], bu, s[0]);
+            s[1] = fmaf(wx[b], bv, s[1]);
+            s[2] = fmaf(dwx[b], bu, s[2]);
+            s[3] = fmaf(dwx[b], bv, s[3]);
+            s[4] = fmaf(wx[b], du, s[4]);
+            s[5] = fmaf(wx[b], dv, s[5]);
+        }
+        acc[0] = fmaf(wt, s[0], acc[0]);
+        acc[1] = fmaf(wt, s[1], acc[1]);
+        acc[2] = fmaf(dwt, s[0], acc[2]);
+        acc[3] = fmaf(dwt, s[1], acc[3]);
+        acc[4] = fmaf(wt, s[2], acc[4]);
+        acc[5] = fmaf(wt, s[3], acc[5]);
+        acc[6] = fmaf(wt, s[4], acc[6]);
+        acc[7] = fmaf(wt, s[5], acc[7]);
+    }
+    if (LP > 1) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned gmask = ((1u << LP) - 1u) << (lane & ~(unsigned)(LP - 1));
+#pragma unroll
+        for (int o = 1; o < LP; o <<= 1)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc[k] += __shfl_xor_sync(gmask, acc[k], o);
+    }
+    *u = fmaf(dl[2], acc[6], fmaf(dl[1], acc[4], fmaf(dl[0], acc[2], acc[0])));
+    *v = fmaf(dl[2], acc[7], fmaf(dl[1], acc[5], fmaf(dl[0], acc[3], acc[1])));
+}
+
 // EXACT: all three axes have float nodes (AxisF::exact): the cell search skips
 // the compensated node sums (same results).
-template <int SPH, int LP_, bool EXACT = false>
+// XM: extrapolation mode outside the grid box (0 "constant": zero velocity,
+// 1 "nearest", 2 "linear"; the definitions of spline_eval_uv64).
+template <int SPH, int LP_, bool EXACT = false, int XM = 0>
 struct FlowSpline32 {
     static constexpr int LP = LP_;
     SplineGridF g;
@@ -359,19 +437,24 @@ struct FlowSpline32 {
             xh = fmaf(-360.0f, k, xh);  // exact no-op for k = 0
         }
         float ft, fx, fy, wx[4], wy[4];
+        float dl[3] = {0.0f, 0.0f, 0.0f};
         bool out = false;
-        int it = locate_pair<EXACT>(g.ax[0], p0 * th, p0 * ts, &ft, &out);
-        int ix = locate_pair<EXACT>(g.ax[1], xh, ys[0], &fx, &out);
-        int iy = locate_pair<EXACT>(g.ax[2], yh[1], ys[1], &fy, &out);
-        if (out) {  // the lanes of a group agree: they hold the same particle
+        int it = locate_pair<EXACT, XM>(g.ax[0], p0 * th, p0 * ts, &ft, &out, dl);
+        int ix = locate_pair<EXACT, XM>(g.ax[1], xh, ys[0], &fx, &out, dl + 1);
+        int iy = locate_pair<EXACT, XM>(g.ax[2], yh[1], ys[1], &fy, &out, dl + 2);
+        if (XM == 0 && out) {  // the lanes of a group agree: they hold the same particle
             dy[0] = 0.0f;
             dy[1] = 0.0f;
             return;
         }
-        bspline_w32(fx, wx);
-        bspline_w32(fy, wy);
         float u, v;
-        spline_eval_uv32<LP>(g, c, it, ix, iy, ft, wx, wy, &u, &v);
+        if (XM == 2 && out) {
+            spline_eval_uv32_lin<LP>(g, c, it, ix, iy, ft, fx, fy, dl, &u, &v);
+        } else {
+            bspline_w32(fx, wx);
+            bspline_w32(fy, wy);
+            spline_eval_uv32<LP>(g, c, it, ix, iy, ft, wx, wy, &u, &v);
+        }
         if (SPH == 1 || SPH == 2) {
             float lat = yh[1] + ys[1];
             // approximate reciprocal (2 ulp): far inside the FP32 stage error

@@ -78,45 +78,37 @@ __device__ __forceinline__ void bspline_w64(double t, double* w)
     w[3] = (1.0 / 6.0) * t3 + (0.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
 }
 
-// Cell index and fractional offset along axis d of a coordinate on or inside
-// the grid box (clamped into [a, b]).
-__device__ __forceinline__ int spline_locate64(const SplineGrid& g, int d, int extrap,
-                                               double x, double* t)
+// derivative of the basis with respect to the offset t
+__device__ __forceinline__ void bspline_dw64(double t, double* w)
 {
-    if (extrap == 0) {
-        if (x < g.a[d]) x = g.a[d];
-        if (x > g.b[d]) x = g.b[d];
-    }
+    double t2 = t * t;
+    w[0] = (-3.0 / 6.0) * t2 + (6.0 / 6.0) * t + (-3.0 / 6.0);
+    w[1] = (9.0 / 6.0) * t2 + (-12.0 / 6.0) * t + (0.0 / 6.0);
+    w[2] = (-9.0 / 6.0) * t2 + (6.0 / 6.0) * t + (3.0 / 6.0);
+    w[3] = (3.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
+}
+
+// Cell index and fractional offset along axis d of a coordinate on or inside
+// [a, b]; a NaN coordinate takes cell 0 (and a NaN offset).
+__device__ __forceinline__ int spline_locate64(const SplineGrid& g, int d, double x, double* t)
+{
     double u = (x - g.a[d]) * g.dinv[d];
     double fu = floor(u);
     int i;
     if (fu > (double)(g.n[d] - 2)) i = g.n[d] - 2;
-    else if (fu < 0.0) i = 0;
+    else if (!(fu >= 0.0)) i = 0;
     else i = (int)fu;
     *t = u - (double)i;
     return i;
 }
 
-// Tricubic evaluation of the interleaved (u, v) coefficient block.
-__device__ __forceinline__ void spline_eval_uv64(const SplineGrid& g, const double2* __restrict__ c,
-                                                 int extrap, double t, double x, double y,
-                                                 double* u, double* v)
+// sum_a w0[a] sum_b w1[b] sum_c w2[c] C[it+a, ix+b, iy+c] of the interleaved
+// (u, v) coefficient block
+__device__ __forceinline__ void spline_sum_uv64(const SplineGrid& g, const double2* __restrict__ c,
+                                                int it, int ix, int iy, const double* w0,
+                                                const double* w1, const double* w2, double* u,
+                                                double* v)
 {
-    // extrap 0 ("constant", the interpolation package's CONSTANT option): the
-    // interpolant is 0 strictly outside the grid box
-    if (extrap == 0 && (t < g.a[0] || t > g.b[0] || x < g.a[1] || x > g.b[1] || y < g.a[2] ||
-                        y > g.b[2])) {
-        *u = 0.0;
-        *v = 0.0;
-        return;
-    }
-    double ft, fx, fy, wt[4], wx[4], wy[4];
-    int it = spline_locate64(g, 0, extrap, t, &ft);
-    int ix = spline_locate64(g, 1, extrap, x, &fx);
-    int iy = spline_locate64(g, 2, extrap, y, &fy);
-    bspline_w64(ft, wt);
-    bspline_w64(fx, wx);
-    bspline_w64(fy, wy);
     double au = 0.0, av = 0.0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -125,24 +117,73 @@ __device__ __forceinline__ void spline_eval_uv64(const SplineGrid& g, const doub
         for (int b = 0; b < 4; ++b) {
             const double2* row = c + (size_t)(it + a) * g.st + (size_t)(ix + b) * g.sx + iy;
             double2 r0 = __ldg(row), r1 = __ldg(row + 1), r2 = __ldg(row + 2), r3 = __ldg(row + 3);
-            double bu = wy[0] * r0.x + wy[1] * r1.x + wy[2] * r2.x + wy[3] * r3.x;
-            double bv = wy[0] * r0.y + wy[1] * r1.y + wy[2] * r2.y + wy[3] * r3.y;
-            su += wx[b] * bu;
-            sv += wx[b] * bv;
+            double bu = w2[0] * r0.x + w2[1] * r1.x + w2[2] * r2.x + w2[3] * r3.x;
+            double bv = w2[0] * r0.y + w2[1] * r1.y + w2[2] * r2.y + w2[3] * r3.y;
+            su += w1[b] * bu;
+            sv += w1[b] * bv;
         }
-        au += wt[a] * su;
-        av += wt[a] * sv;
+        au += w0[a] * su;
+        av += w0[a] * sv;
     }
     *u = au;
     *v = av;
 }
 
-template <int SPH>
+// Tricubic evaluation of (u, v) at (t, x, y) with extrapolation mode XM, the
+// extrap_mode of the interpolation package's eval_spline that the reference
+// passes through (flows.py:121):
+//   0 "constant": 0 strictly outside the grid box;
+//   1 "nearest":  each coordinate clamped into its axis' [a, b];
+//   2 "linear":   the value at the clamped point plus, for each clamped axis
+//                 (t, x, y in that order), the derivative along that axis at
+//                 the clamped point times the distance beyond the box.
+template <int XM>
+__device__ __forceinline__ void spline_eval_uv64(const SplineGrid& g, const double2* __restrict__ c,
+                                                 double t, double x, double y, double* u,
+                                                 double* v)
+{
+    if (XM == 0 && (t < g.a[0] || t > g.b[0] || x < g.a[1] || x > g.b[1] || y < g.a[2] ||
+                    y > g.b[2])) {
+        *u = 0.0;
+        *v = 0.0;
+        return;
+    }
+    const double vv[3] = {t, x, y};
+    double dl[3], f[3], w[3][4];
+    int i[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double cl = vv[d];
+        if (XM != 0) cl = vv[d] < g.a[d] ? g.a[d] : (vv[d] > g.b[d] ? g.b[d] : vv[d]);
+        dl[d] = vv[d] - cl;
+        i[d] = spline_locate64(g, d, cl, &f[d]);
+        bspline_w64(f[d], w[d]);
+    }
+    double au, av;
+    spline_sum_uv64(g, c, i[0], i[1], i[2], w[0], w[1], w[2], &au, &av);
+    if (XM == 2) {
+#pragma unroll 1
+        for (int d = 0; d < 3; ++d) {
+            if (dl[d] == 0.0 || isnan(dl[d])) continue;
+            double dw[4], gu, gv;
+            bspline_dw64(f[d], dw);
+            spline_sum_uv64(g, c, i[0], i[1], i[2], d == 0 ? dw : w[0], d == 1 ? dw : w[1],
+                            d == 2 ? dw : w[2], &gu, &gv);
+            const double s = dl[d] * g.dinv[d];
+            au = au + s * gu;
+            av = av + s * gv;
+        }
+    }
+    *u = au;
+    *v = av;
+}
+
+// XM: extrapolation mode (0 constant, 1 nearest, 2 linear)
+template <int SPH, int XM = 0>
 struct FlowSpline64 {
     SplineGrid g;
     const double2* __restrict__ c;
     double r;
-    int extrap;
 
     __device__ __forceinline__ void operator()(double t, const double* y, double* dy,
                                                const Params& P) const
@@ -153,11 +194,11 @@ struct FlowSpline64 {
         if (SPH == 1 || SPH == 2) {
             double xx = SPH == 1 ? py_fmod(y[0] - 180.0, 360.0) - 180.0 : py_fmod(y[0], 360.0);
             double yy = y[1];
-            spline_eval_uv64(g, c, extrap, tt, xx, yy, &u, &v);
+            spline_eval_uv64<XM>(g, c, tt, xx, yy, &u, &v);
             dy[0] = p[0] * u * 180.0 / (NBCS_PI * r * nbcs_cos_deg(yy));
             dy[1] = p[0] * v * 180.0 / (NBCS_PI * r);
         } else {
-            spline_eval_uv64(g, c, extrap, tt, y[0], y[1], &u, &v);
+            spline_eval_uv64<XM>(g, c, tt, y[0], y[1], &u, &v);
             dy[0] = p[0] * u;
             dy[1] = p[0] * v;
         }

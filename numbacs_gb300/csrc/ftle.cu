@@ -270,6 +270,7 @@ extern "C" int nbcs_ftle_grid_2d(const double* flowmap, int32_t nx, int32_t ny, 
                                  double dx, double dy, const uint8_t* mask, double* ftle,
                                  void* stream)
 {
+    NBCS_RANGE();
     int rc = check_fm(flowmap, nx, ny);
     if (rc) return rc;
     long n = (long)nx * ny;
@@ -285,6 +286,7 @@ extern "C" int nbcs_ftle_grid_2d(const double* flowmap, int32_t nx, int32_t ny, 
 extern "C" int nbcs_c_eig_2d(const double* flowmap, int32_t nx, int32_t ny, double dx, double dy,
                              const uint8_t* mask, double* evals, double* evecs, void* stream)
 {
+    NBCS_RANGE();
     int rc = check_fm(flowmap, nx, ny);
     if (rc) return rc;
     long n = (long)nx * ny;
@@ -302,6 +304,7 @@ extern "C" int nbcs_c_eig_aux_2d(const double* flowmap_aux, int32_t nx, int32_t 
                                  int32_t eig_main, double dx, double dy, double h,
                                  const uint8_t* mask, double* evals, double* evecs, void* stream)
 {
+    NBCS_RANGE();
     if (nx < 0 || ny < 0) return set_error(NBCS_ERR_INVALID, "c_eig_aux: negative grid size");
     long n = (long)nx * ny;
     if (n == 0) return NBCS_OK;
@@ -320,6 +323,7 @@ extern "C" int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, 
                                  double dx, double dy, const uint8_t* mask, double* ftle,
                                  double* evec_max, void* stream)
 {
+    NBCS_RANGE();
     int rc = check_fm(flowmap, nx, ny);
     if (rc) return rc;
     long n = (long)nx * ny;
@@ -336,6 +340,7 @@ extern "C" int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, 
 extern "C" int nbcs_ftle_from_eig(const double* eigval, int64_t n, int64_t stride, double T,
                                   double* ftle, void* stream)
 {
+    NBCS_RANGE();
     if (n < 0 || stride < 1) return set_error(NBCS_ERR_INVALID, "ftle_from_eig: bad n/stride");
     if (n == 0) return NBCS_OK;
     if (!eigval || !ftle) return set_error(NBCS_ERR_INVALID, "ftle_from_eig: NULL array");

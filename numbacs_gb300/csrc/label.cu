@@ -168,6 +168,7 @@ extern "C" size_t nbcs_label8_scratch_bytes(int32_t nx, int32_t ny)
 extern "C" int nbcs_label8(const uint8_t* mask, int32_t nx, int32_t ny, int32_t* labels,
                            int32_t* nlabels, void* scratch, size_t scratch_bytes, void* stream)
 {
+    NBCS_RANGE();
     if (nx < 0 || ny < 0 || (long)nx * ny > 0x7fffffffL)
         return set_error(NBCS_ERR_INVALID, "label8: grid size out of range");
     const long n = (long)nx * ny;

@@ -299,6 +299,9 @@ static int launch_learned(const nbcs_flow* flow, const FlowmapArgs& a, const Mlp
 {
     if (flow->kind != NBCS_FLOW_SPLINE2D)
         return set_error(NBCS_ERR_UNSUPPORTED, "the learned step proposer needs a spline flow");
+    if (flow->extrap != 0)
+        return set_error(NBCS_ERR_UNSUPPORTED,
+                         "the learned step proposer takes extrap_mode 'constant' only");
     SplineGridF g = make_grid_f(flow->grid);
     const float* c = flow->coef_uv32;
     float kd = (float)(180.0 / (3.141592653589793 * flow->r));
@@ -343,6 +346,7 @@ extern "C" int nbcs_flowmap_log_steps(const nbcs_flow* flow, double t0, double T
                                       float sample, uint32_t seed, float* feats, float* targets,
                                       int64_t capacity, unsigned long long* count, void* stream)
 {
+    NBCS_RANGE();
     int rc = validate_flow(flow, params, np, NBCS_PREC_MIXED);
     if (rc) return rc;
     if (nx < 0 || ny < 0 || !x || !y || !count || capacity < 0 || (capacity > 0 && (!feats || !targets)))

@@ -324,6 +324,7 @@ extern "C" int nbcs_mlp_param_count(void) { return kMlpParams; }
 
 extern "C" int nbcs_mlp_pack(const float* params, void* blob, void* stream)
 {
+    NBCS_RANGE();
     if (!params || !blob || (reinterpret_cast<uintptr_t>(blob) & 15))
         return set_error(NBCS_ERR_INVALID, "mlp_pack: NULL or misaligned arguments");
     mlp_pack_kernel<<<8, 256, 0, as_stream(stream)>>>(params, static_cast<MlpBlob*>(blob));
@@ -334,6 +335,7 @@ extern "C" int nbcs_mlp_pack(const float* params, void* blob, void* stream)
 extern "C" int nbcs_mlp_predict(const void* blob, const float* feats, int64_t n, float* out,
                                 void* stream)
 {
+    NBCS_RANGE();
     if (n < 0 || (n > 0 && (!blob || !feats || !out)))
         return set_error(NBCS_ERR_INVALID, "mlp_predict: bad arguments");
     if (n == 0) return NBCS_OK;
@@ -348,6 +350,7 @@ extern "C" int nbcs_mlp_predict(const void* blob, const float* feats, int64_t n,
 extern "C" int nbcs_mlp_grad(const void* blob, const float* feats, const float* targets, int64_t n,
                              float* grad, float* loss, void* stream)
 {
+    NBCS_RANGE();
     if (n <= 0 || !blob || !feats || !targets || !grad || !loss)
         return set_error(NBCS_ERR_INVALID, "mlp_grad: bad arguments");
     cudaStream_t s = as_stream(stream);
@@ -369,6 +372,7 @@ extern "C" int nbcs_mlp_adam(float* params, float* m, float* v, const float* gra
                              float beta1, float beta2, float eps, int32_t step, void* blob,
                              void* stream)
 {
+    NBCS_RANGE();
     if (!params || !m || !v || !grad || step < 1)
         return set_error(NBCS_ERR_INVALID, "mlp_adam: bad arguments");
     const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "../../include/nbcs.h"
@@ -26,6 +27,17 @@ void count_launch();
         ::nbcs::count_launch();              \
         NBCS_CUDA_TRY(cudaGetLastError());   \
     } while (0)
+
+// NVTX range over one C-ABI call, so that a timeline (Nsight Systems, or ncu
+// with --nvtx) shows which entry point issued which kernels.  NVTX3 is
+// header-only: without an attached tool each push/pop is a load and a branch.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define NBCS_RANGE() ::nbcs::NvtxRange nbcs_range_(__func__)
 
 // Number of SMs of the current device (cached per device).
 int sm_count();

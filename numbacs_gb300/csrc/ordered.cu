@@ -402,6 +402,7 @@ extern "C" int nbcs_order_ridges(const double* f, const double* evec_max, const 
                                  double c, double* pts_out, int64_t max_pts, int64_t* ridge_len_out,
                                  int64_t max_ridges, int64_t* n_pts, int64_t* n_ridges)
 {
+    NBCS_RANGE();
     if (nx < 3 || ny < 3 || !f || !evec_max || !x || !y || !ridge_mask || !r_pts || !n_pts ||
         !n_ridges)
         return set_error(NBCS_ERR_INVALID, "order_ridges: need nx, ny >= 3 and non-NULL arrays");

@@ -34,6 +34,7 @@ extern "C" unsigned long long nbcs_launch_count(void) { return g_launches.load()
 extern "C" int nbcs_probe_fma(int32_t precision, int64_t iters, void* sink, double* flops,
                               void* stream)
 {
+    NBCS_RANGE();
     if (iters < 1 || !sink || !flops) return set_error(NBCS_ERR_INVALID, "probe_fma: bad arguments");
     const int threads = 256;
     const long blocks = (long)sm_count() * 8;

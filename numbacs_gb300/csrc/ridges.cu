@@ -482,6 +482,7 @@ extern "C" size_t nbcs_percentile_scratch_bytes(int64_t n)
 extern "C" int nbcs_percentile(const double* f, int64_t n, double q, double* out, void* scratch,
                                size_t scratch_bytes, void* stream)
 {
+    NBCS_RANGE();
     if (n < 1 || !f || !out) return set_error(NBCS_ERR_INVALID, "percentile: empty input or NULL");
     if (!(q >= 0.0 && q <= 100.0)) return set_error(NBCS_ERR_INVALID, "percentile: q outside [0, 100]");
     if (!scratch || scratch_bytes < sizeof(SelScratch))
@@ -568,6 +569,7 @@ extern "C" int nbcs_ridge_pts(const double* f, const double* evec_max, const dou
                               uint8_t* mask_out, double* rpts_full, double* pts_out,
                               int64_t* n_out, void* scratch, size_t scratch_bytes, void* stream)
 {
+    NBCS_RANGE();
     return ridge_run(f, evec_max, x, nx, y, ny, NAN, NAN, sdd_thresh, true, percentile, 0.0,
                      mask_out, rpts_full, pts_out, n_out, scratch, scratch_bytes, stream);
 }
@@ -578,6 +580,7 @@ extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, cons
                                    double* rpts_full, double* pts_out, int64_t* n_out,
                                    void* scratch, size_t scratch_bytes, void* stream)
 {
+    NBCS_RANGE();
     if (!(dx > 0.0 || dx < 0.0) || !(dy > 0.0 || dy < 0.0))
         return set_error(NBCS_ERR_INVALID, "ridge_pts_fmin: dx, dy must be nonzero");
     return ridge_run(f, evec_max, x, nx, y, ny, dx, dy, sdd_thresh, false, 0.0, f_min, mask_out,
@@ -598,6 +601,8 @@ extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, cons
 // The array's name is only a host-side stand-in, so the device address is
 // looked up with cudaGetSymbolAddress, once per device, on the first call made
 // with that device current (make that first call before any stream capture).
+// The address is cached per device ordinal, i.e. for the runtime's primary
+// context; it is not refreshed after cudaDeviceReset.
 // Every call shares the array and leaves its contents behind; the kernels
 // re-initialise everything they read (the selection state and histogram, the
 // per-block counts, offsets and mask), and calls whose work overlaps on the
@@ -645,6 +650,7 @@ extern "C" int nbcs_ridge_pts_noalloc(const double* f, const double* evec_max, c
                                       double percentile, uint8_t* mask_out, double* rpts_full,
                                       double* pts_out, int64_t* n_out, void* stream)
 {
+    NBCS_RANGE();
     if (nx < 0 || ny < 0 || (long)nx * ny > NBCS_RIDGE_NOALLOC_MAX_POINTS)
         return set_error(NBCS_ERR_INVALID,
                          "ridge_pts_noalloc: %d x %d grid exceeds the fixed scratch limit of %ld "

@@ -132,6 +132,7 @@ extern "C" int nbcs_spline_prefilter_3d(const double* f, int32_t nt, int32_t nx,
                                         double* coef, void* scratch, size_t scratch_bytes,
                                         void* stream)
 {
+    NBCS_RANGE();
     if (nt < 1 || nx < 1 || ny < 1 || !f || !coef)
         return set_error(NBCS_ERR_INVALID, "prefilter: bad sizes or NULL arrays");
     if (nt > kMaxLine || nx > kMaxLine || ny > kMaxLine)
@@ -155,6 +156,7 @@ extern "C" int nbcs_spline_prefilter_3d(const double* f, int32_t nt, int32_t nx,
 extern "C" int nbcs_spline_pack_uv(const double* cu, const double* cv, int64_t n, double* coef_uv,
                                    float* coef_uv32, void* stream)
 {
+    NBCS_RANGE();
     if (n < 0 || (n > 0 && (!cu || !cv || !coef_uv)))
         return set_error(NBCS_ERR_INVALID, "pack_uv: bad arguments");
     if ((reinterpret_cast<uintptr_t>(coef_uv) & 15) || (reinterpret_cast<uintptr_t>(coef_uv32) & 31))

@@ -148,7 +148,8 @@ def get_interp_arrays_2D(tvals, xvals, yvals, U, V):
     return grid_vel, D.finish(Cu, as_torch), D.finish(Cv, as_torch)
 
 
-_EXTRAP = {"constant": 0}
+# extrap_mode -> nbcs_flow.extrap (the interpolation package's option names)
+_EXTRAP = {"constant": 0, "nearest": 1, "linear": 2}
 
 
 def get_flow_2D(grid_vel, C_eval_u, C_eval_v, spherical=0, extrap_mode="constant", r=6371.0):
@@ -156,13 +157,26 @@ def get_flow_2D(grid_vel, C_eval_u, C_eval_v, spherical=0, extrap_mode="constant
 
     The reference closes a numba cfunc over the coefficient arrays; here the
     coefficients are packed once into interleaved (u, v) FP64 and FP32 device
-    arrays owned by the returned :class:`Flow`.  ``extrap_mode="constant"``
-    holds the velocity at its value on the grid boundary (coordinates are
-    clamped into the grid box).
+    arrays owned by the returned :class:`Flow`.
+
+    ``extrap_mode`` decides the velocity at a point (t, x, y) outside the grid
+    box, as the reference passes it on to the interpolation package's
+    ``eval_spline``:
+
+    * ``"constant"``: zero velocity, so a particle that leaves the box stops;
+    * ``"nearest"``: the velocity at the nearest point of the box (each
+      coordinate clamped into its axis' range);
+    * ``"linear"``: that value continued to first order, plus the spline's
+      derivative along each clamped axis times the distance beyond the box.
+
+    "constant" is pinned by the reference's composition fixtures; no fixture
+    pins "nearest" or "linear", whose definition here is the CPU oracle's
+    (the GPU integrators match it bit for bit in FP64).  The batched kernels
+    (:class:`batch.FTLEBatch`) run such flows through the per-field schedule.
     """
     D.require_cuda()
     if extrap_mode not in _EXTRAP:
-        raise NotImplementedError("extrap_mode %r is not supported (only 'constant')" % extrap_mode)
+        raise ValueError("extrap_mode must be one of %s, got %r" % (sorted(_EXTRAP), extrap_mode))
     if spherical not in (0, 1, 2):
         raise ValueError("spherical must be 0, 1 or 2")
     cu, cv = D.to_dev(C_eval_u), D.to_dev(C_eval_v)

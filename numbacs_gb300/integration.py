@@ -201,6 +201,11 @@ def flowmap_composition_initial(funcptr, t0, T, h, x, y, grid, params, *, stream
     xd, yd = D.to_dev(x), D.to_dev(y)
     nT = abs(round(T / h))
     fms = D.empty((nT, xd.numel(), yd.numel(), 2))
+    # every per-map call must stay asynchronous for the streams to overlap:
+    # device inputs and a device `out` keep flowmap_grid_2D from reading its
+    # status back, and a host mask is copied to the device once, here
+    if kwargs.get("mask") is not None:
+        kwargs["mask"] = D.mask_to_dev(kwargs["mask"])
     main = torch.cuda.current_stream()
     pool = [torch.cuda.Stream() for _ in range(max(1, min(int(streams), nT)))]
     for s in pool:

@@ -90,54 +90,90 @@ static void bspline_weights(double t, double w[4])
     w[3] = (1.0 / 6.0) * t3 + (0.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
 }
 
-/* cell index and fractional offset along one axis (a, b, n); the coordinate
- * is clamped into [a, b] (only points on or inside the box get here when
- * extrap is 0) */
-static int spline_locate(double a, double b, int n, int extrap, double x, double* t)
+/* derivative of the basis with respect to the offset t (the rows above
+ * differentiated: [3t^2, 2t, 1] times the t^3, t^2, t coefficients) */
+static void bspline_dweights(double t, double w[4])
 {
-    if (extrap == 0) {
-        if (x < a) x = a;
-        if (x > b) x = b;
-    }
+    double t2 = t * t;
+    w[0] = (-3.0 / 6.0) * t2 + (6.0 / 6.0) * t + (-3.0 / 6.0);
+    w[1] = (9.0 / 6.0) * t2 + (-12.0 / 6.0) * t + (0.0 / 6.0);
+    w[2] = (-9.0 / 6.0) * t2 + (6.0 / 6.0) * t + (3.0 / 6.0);
+    w[3] = (3.0 / 6.0) * t2 + (0.0 / 6.0) * t + (0.0 / 6.0);
+}
+
+/* cell index and fractional offset along one axis (a, b, n) of a coordinate
+ * on or inside [a, b]; a NaN coordinate takes cell 0 (and a NaN offset) */
+static int spline_locate(double a, double b, int n, double x, double* t)
+{
     double dinv = (double)(n - 1) / (b - a);
     double u = (x - a) * dinv;
     double fu = floor(u);
     int i;
     if (fu > (double)(n - 2)) i = n - 2;
-    else if (fu < 0.0) i = 0;
+    else if (!(fu >= 0.0)) i = 0;
     else i = (int)fu;
     *t = u - (double)i;
     return i;
 }
 
-double orc_eval_spline_3d(const double* g, const double* c, int extrap,
-                          double t, double x, double y)
+/* sum_a w0[a] sum_b w1[b] sum_c w2[c] C[it+a, ix+b, iy+c] */
+static double spline_sum(const double* c, int st, int sx, int it, int ix, int iy,
+                         const double* w0, const double* w1, const double* w2)
 {
-    int nt = (int)g[2], nx = (int)g[5], ny = (int)g[8];
-    int sx = ny + 2, st = (nx + 2) * (ny + 2);
-    /* extrap 0 ("constant", the interpolation package's CONSTANT option): the
-     * interpolant is 0 strictly outside the grid box.  Pinned through
-     * flowmap_composition's fixtures (integration.py:630-640 evaluate
-     * eval_linear(..., xto.CONSTANT); wall points that a map leaves 1 ulp
-     * outside [0, 2] compose to 0 there); eval_spline takes the same option. */
-    if (extrap == 0 && (t < g[0] || t > g[1] || x < g[3] || x > g[4] || y < g[6] || y > g[7]))
-        return 0.0;
-    double ft, fx, fy, wt[4], wx[4], wy[4];
-    int it = spline_locate(g[0], g[1], nt, extrap, t, &ft);
-    int ix = spline_locate(g[3], g[4], nx, extrap, x, &fx);
-    int iy = spline_locate(g[6], g[7], ny, extrap, y, &fy);
-    bspline_weights(ft, wt);
-    bspline_weights(fx, wx);
-    bspline_weights(fy, wy);
     double acc = 0.0;
     for (int a = 0; a < 4; ++a) {
         double sa = 0.0;
         for (int b = 0; b < 4; ++b) {
             const double* row = c + (size_t)(it + a) * st + (size_t)(ix + b) * sx + iy;
-            double sb = wy[0] * row[0] + wy[1] * row[1] + wy[2] * row[2] + wy[3] * row[3];
-            sa += wx[b] * sb;
+            double sb = w2[0] * row[0] + w2[1] * row[1] + w2[2] * row[2] + w2[3] * row[3];
+            sa += w1[b] * sb;
         }
-        acc += wt[a] * sa;
+        acc += w0[a] * sa;
+    }
+    return acc;
+}
+
+/* Tricubic B-spline value at (t, x, y) with the extrapolation modes of the
+ * interpolation package's eval_spline (flows.py:121 passes extrap_mode
+ * through unchanged):
+ *   0 "constant": 0 strictly outside the grid box.  Pinned through
+ *     flowmap_composition's fixtures (integration.py:630-640 evaluate
+ *     eval_linear(..., xto.CONSTANT); wall points that a map leaves 1 ulp
+ *     outside [0, 2] compose to 0 there); eval_spline takes the same option.
+ *   1 "nearest": each coordinate clamped into its axis' [a, b], then
+ *     evaluated there.
+ *   2 "linear": the value at that clamped point plus, for every axis whose
+ *     coordinate was clamped (t, then x, then y), the spline's derivative
+ *     along that axis at the clamped point times the distance beyond the
+ *     box (first-order continuation from the box surface).
+ * No fixture of the reference pins modes 1 and 2; this definition is the
+ * behaviour the GPU path is tested against. */
+double orc_eval_spline_3d(const double* g, const double* c, int extrap,
+                          double t, double x, double y)
+{
+    int n[3] = {(int)g[2], (int)g[5], (int)g[8]};
+    int sx = n[2] + 2, st = (n[1] + 2) * (n[2] + 2);
+    if (extrap == 0 && (t < g[0] || t > g[1] || x < g[3] || x > g[4] || y < g[6] || y > g[7]))
+        return 0.0;
+    double v[3] = {t, x, y}, cl[3], dl[3], f[3], w[3][4];
+    int i[3];
+    for (int d = 0; d < 3; ++d) {
+        double a = g[3 * d], b = g[3 * d + 1];
+        cl[d] = v[d] < a ? a : (v[d] > b ? b : v[d]);
+        dl[d] = v[d] - cl[d];
+        i[d] = spline_locate(a, b, n[d], cl[d], &f[d]);
+        bspline_weights(f[d], w[d]);
+    }
+    double acc = spline_sum(c, st, sx, i[0], i[1], i[2], w[0], w[1], w[2]);
+    if (extrap == 2) {
+        for (int d = 0; d < 3; ++d) {
+            if (dl[d] == 0.0 || dl[d] != dl[d]) continue;
+            double dw[4], dinv = (double)(n[d] - 1) / (g[3 * d + 1] - g[3 * d]);
+            bspline_dweights(f[d], dw);
+            double gd = spline_sum(c, st, sx, i[0], i[1], i[2], d == 0 ? dw : w[0],
+                                   d == 1 ? dw : w[1], d == 2 ? dw : w[2]);
+            acc = acc + (dl[d] * dinv) * gd;
+        }
     }
     return acc;
 }
@@ -151,7 +187,8 @@ static void rhs_spline(const orc_flow* fl, double t, const double* y, double* dy
         double yy = y[1];
         double u = orc_eval_spline_3d(fl->grid, fl->cu, fl->extrap, tt, xx, yy);
         double v = orc_eval_spline_3d(fl->grid, fl->cv, fl->extrap, tt, xx, yy);
-        dy[0] = p[0] * u * 180.0 / (PI_D * fl->r * nbcs_cos_deg(yy));
+        double cy = fl->libm ? cos(yy * PI_D / 180.0) : nbcs_cos_deg(yy);
+        dy[0] = p[0] * u * 180.0 / (PI_D * fl->r * cy);
         dy[1] = p[0] * v * 180.0 / (PI_D * fl->r);
     } else {
         double u = orc_eval_spline_3d(fl->grid, fl->cu, fl->extrap, tt, y[0], y[1]);
@@ -285,7 +322,8 @@ static double hinit(const orc_flow* fl, const double* p, double x, const double*
     der2 = sqrt(der2) / h;
     der12 = dmax(fabs(der2), sqrt(dnf));
     if (der12 <= 1.0e-15) h1 = dmax(1.0e-6, fabs(h) * 1.0e-3);
-    else h1 = nbcs_root8(0.01 / der12); /* (0.01/der12)^(1/iord), iord = 8 */
+    else if (fl->libm) h1 = pow(0.01 / der12, 1.0 / 8.0); /* (0.01/der12)^(1/iord), iord = 8 */
+    else h1 = nbcs_root8(0.01 / der12);
     h = dmin(100.0 * fabs(h), dmin(h1, hmax));
     return dsign(h, posneg);
 }
@@ -385,7 +423,7 @@ int orc_dop853(const orc_flow* fl, const double* p, double x, double xend,
         if (isnan(err)) { status = ORC_NONFINITE; break; }
         /* new step size, fac1 <= hnew/h <= fac2 */
         /* err^expo1 with expo1 = 1/8 (beta = 0, so facold^beta = 1) */
-        fac11 = nbcs_root8(err);
+        fac11 = fl->libm ? pow(err, 0.125) : nbcs_root8(err);
         fac = fac11;
         fac = dmax(facc2, dmin(facc1, fac / safe));
         hnew = h / fac;

@@ -35,11 +35,18 @@ enum {
 typedef struct {
     int kind;          /* ORC_FLOW_* */
     int spherical;     /* spline only: 0 planar, 1 lon in [-180,180), 2 lon in [0,360) */
-    int extrap;        /* spline only: 0 = constant (coordinates clamped to the grid box) */
+    int extrap;        /* spline only, outside the grid box: 0 constant (zero), 1 nearest,
+                          2 linear (orc_eval_spline_3d) */
     double r;          /* spline only: sphere radius used for the km -> degree conversion */
     double grid[9];    /* spline only: t0,t1,nt, x0,x1,nx, y0,y1,ny */
     const double* cu;  /* spline only: coefficients (nt+2, nx+2, ny+2), C order */
     const double* cv;
+    /* 0: the deterministic helpers the GPU library also uses (err^(1/8) as
+     * three square roots, the Taylor-series cos of the spherical metric), so
+     * that GPU and oracle can be compared bit for bit; 1: the reference's
+     * literal libm calls (pow(err, 1/8) as in Hairer's dop853, cos(lat*pi/180)
+     * as in flows.py:180), to measure how far those helpers move results */
+    int libm;
 } orc_flow;
 
 /* the deterministic helpers of detmath.h (exposed for their accuracy test) */

@@ -54,7 +54,7 @@ _lib = None
 class _Flow(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("spherical", ctypes.c_int), ("extrap", ctypes.c_int),
                 ("r", ctypes.c_double), ("grid", ctypes.c_double * 9),
-                ("cu", ctypes.c_void_p), ("cv", ctypes.c_void_p)]
+                ("cu", ctypes.c_void_p), ("cv", ctypes.c_void_p), ("libm", ctypes.c_int)]
 
 
 def _dp(a):
@@ -93,7 +93,8 @@ def lib():
 class Flow:
     """Oracle-side flow description (analytic kind, or spline coefficients)."""
 
-    def __init__(self, kind, grid=None, cu=None, cv=None, spherical=0, extrap=0, r=6371.0):
+    def __init__(self, kind, grid=None, cu=None, cv=None, spherical=0, extrap=0, r=6371.0,
+                 libm=False):
         self.kind = kind
         self.cu = None if cu is None else np.ascontiguousarray(cu, dtype=np.float64)
         self.cv = None if cv is None else np.ascontiguousarray(cv, dtype=np.float64)
@@ -108,22 +109,25 @@ class Flow:
                 self.s.grid[k] = flat[k]
         self.s.cu = _dp(self.cu)
         self.s.cv = _dp(self.cv)
+        # libm=True: the reference's literal pow / cos calls instead of the
+        # deterministic helpers shared with the GPU library (oracle.h)
+        self.s.libm = int(bool(libm))
 
     @property
     def ptr(self):
         return ctypes.byref(self.s)
 
 
-def double_gyre():
-    return Flow(FLOW_DOUBLE_GYRE)
+def double_gyre(libm=False):
+    return Flow(FLOW_DOUBLE_GYRE, libm=libm)
 
 
-def bickley_jet():
-    return Flow(FLOW_BICKLEY)
+def bickley_jet(libm=False):
+    return Flow(FLOW_BICKLEY, libm=libm)
 
 
-def spline_flow(grid, cu, cv, spherical=0, extrap=0, r=6371.0):
-    return Flow(FLOW_SPLINE2D, grid, cu, cv, spherical, extrap, r)
+def spline_flow(grid, cu, cv, spherical=0, extrap=0, r=6371.0, libm=False):
+    return Flow(FLOW_SPLINE2D, grid, cu, cv, spherical, extrap, r, libm)
 
 
 def rhs(flow, t, y, params):

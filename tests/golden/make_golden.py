@@ -29,7 +29,8 @@ The ``.npy`` files are read with ``allow_pickle=False``; the ``.pkl`` file is re
 with an unpickler that only admits numpy array reconstruction; the test-source
 literals are read with ``ast`` (never executed).
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
+        (or NBCS_REFERENCE_ROOT=<NumbaCS checkout> python tests/golden/make_golden.py)
 """
 import ast
 import io
@@ -121,4 +122,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NBCS_REFERENCE_ROOT", "/root/reference"))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NBCS_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <NumbaCS checkout>  (or set NBCS_REFERENCE_ROOT)")
+    main(root)

@@ -129,6 +129,48 @@ def test_flowmap_parity_spline(nb, orc, spherical):
     _exact(fm, ofm, stats, ostats, "spline%d" % spherical)
 
 
+@pytest.mark.parametrize("extrap", ["nearest", "linear"])
+@pytest.mark.parametrize("spherical", [0, 1])
+def test_flowmap_parity_spline_extrap(nb, orc, extrap, spherical):
+    """extrap_mode "nearest" / "linear": particles seeded across and beyond
+    the grid box, integrated back past the first time sample, so every mode of
+    extrapolation (t, x, y, below and above) is taken.  FP64 bit-identical to
+    the oracle; the mixed path's velocities outside the box within FP32
+    accuracy of the FP64 path's."""
+    t, lon, lat, U, V = _small_geo(orc)
+    if spherical == 0:
+        U, V = U / 111.0, V / 111.0
+    grid, Cu, Cv = nb.get_interp_arrays_2D(t, lon, lat, U, V)
+    og, oCu, oCv = orc.get_interp_arrays_2D(t, lon, lat, U, V)
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=spherical, extrap_mode=extrap)
+    of = orc.spline_flow(og, oCu, oCv, spherical=spherical, extrap={"nearest": 1, "linear": 2}[extrap])
+    xf = np.linspace(lon[0] - 3.0, lon[-1] + 3.0, 41)
+    yf = np.linspace(lat[0] - 2.0, lat[-1] + 2.0, 21)
+    p = np.array([-1.0])
+    fm, st, stats = nb.flowmap_grid_2D(fl, 30.0, -72.0, xf, yf, p, return_status=True,
+                                       return_stats=True)
+    ofm, ost, ostats = orc.flowmap_grid_2D(of, 30.0, -72.0, xf, yf, p, return_status=True)
+    assert np.array_equal(st, ost)
+    _exact(fm, ofm, stats, ostats, "spline%d %s" % (spherical, extrap))
+    # the extrapolated velocities differ from "constant" (zero) outside the box;
+    # rows are (model time, x, y), the solver time is model time / params[0]
+    fl0 = nb.get_flow_2D(grid, Cu, Cv, spherical=spherical)
+    out_pts = np.array([[t[0] - 5.0, lon[5], lat[3]], [t[4], lon[-1] + 1.5, lat[2]],
+                        [t[3], lon[2], lat[0] - 1.0], [t[-1] + 2.0, lon[-1] + 0.7, lat[-1] + 0.4]])
+    ts = out_pts[:, 0] / p[0]
+    v64 = nb.flows.eval_rhs(fl, ts, out_pts[:, 1:], p)
+    assert np.all(np.abs(v64).max(axis=1) > 0)
+    assert np.all(nb.flows.eval_rhs(fl0, ts, out_pts[:, 1:], p) == 0.0)
+    ref = np.array([orc.rhs(of, tq, q[1:], p) for tq, q in zip(ts, out_pts)])
+    assert np.array_equal(v64, ref)
+    v32 = nb.flows.eval_rhs(fl, ts, out_pts[:, 1:], p, precision="mixed")
+    np.testing.assert_allclose(v32, v64, rtol=2e-5, atol=2e-5 * np.abs(v64).max())
+    # mixed flow maps over 12 h (before chaotic growth) within 1e-4 of the box size
+    fm32 = nb.flowmap_grid_2D(fl, 30.0, -12.0, xf, yf, p, rtol=1e-8, atol=1e-10, precision="mixed")
+    fm64 = nb.flowmap_grid_2D(fl, 30.0, -12.0, xf, yf, p, rtol=1e-8, atol=1e-10)
+    assert np.abs(fm32 - fm64).max() <= 1e-4 * (lon[-1] - lon[0])
+
+
 def test_flowmap_torch_in_torch_out(nb, coords_dg):
     x, y = coords_dg
     fl, p, _ = nb.get_predefined_flow("double_gyre")

@@ -27,6 +27,40 @@ def test_flowmap_grid_2D(orc, golden, coords_dg, mask_dg):
     assert np.allclose(fmm.astype(np.float32), apply_mask(golden["fm"], mask_dg))
 
 
+def test_libm_mode_reproduces_golden_and_matches_in_accuracy(orc, golden, coords_dg):
+    """The oracle's default arithmetic uses two deterministic helpers that the
+    GPU library shares (err^(1/8) as three square roots, a Taylor-series cos
+    in the spherical metric) so that the two can be compared bit for bit.  Its
+    libm mode makes the reference's literal pow / cos calls instead.  Both
+    reproduce the golden flow map; on the geophysical spline flow the helpers
+    move trajectories by the flow's sensitivity to one ulp, and both runs are
+    equally accurate against a converged solution."""
+    x, y = coords_dg
+    p = orc.double_gyre_params(1.0)
+    a = orc.flowmap_grid_2D(orc.double_gyre(), 0.0, T_FIX, x, y, p)
+    b = orc.flowmap_grid_2D(orc.double_gyre(libm=True), 0.0, T_FIX, x, y, p)
+    assert np.array_equal(a.astype(np.float32), golden["fm"])
+    assert np.array_equal(b.astype(np.float32), golden["fm"])
+    assert np.abs(a - b).max() <= 1e-10
+    from numbacs_gb300 import workloads as W
+    t, lon, lat, U, V = W.geo_velocity(seed=0, device="cpu")
+    g, cu, cv = orc.get_interp_arrays_2D(t, lon, lat, U, V)
+    lonf, latf = W.geo_ftle_grid(0.2)
+    xs, pm = lonf[::16], np.array([-1.0])
+    det = orc.flowmap_grid_2D(orc.spline_flow(g, cu, cv, spherical=1), 180.0, -72.0, xs, latf, pm,
+                              rtol=1e-7, atol=1e-9)
+    lib = orc.flowmap_grid_2D(orc.spline_flow(g, cu, cv, spherical=1, libm=True), 180.0, -72.0, xs,
+                              latf, pm, rtol=1e-7, atol=1e-9)
+    tr = orc.flowmap_grid_2D(orc.spline_flow(g, cu, cv, spherical=1, libm=True), 180.0, -72.0, xs,
+                             latf, pm, rtol=1e-12, atol=1e-14)
+    bound = 1e-6 * (lon[-1] - lon[0])
+    d = np.abs(det - lib).max(-1)
+    assert np.median(d) <= 1e-3 * bound
+    e_det, e_lib = np.abs(det - tr).max(-1), np.abs(lib - tr).max(-1)
+    assert abs(e_det.mean() - e_lib.mean()) <= 0.05 * e_lib.mean()
+    assert abs(np.quantile(e_det, 0.99) - np.quantile(e_lib, 0.99)) <= 0.05 * np.quantile(e_lib, 0.99)
+
+
 def test_ftle_grid_2D(orc, golden, mask_dg):
     fm = golden["fm"].astype(np.float64)
     f = orc.ftle_grid_2D(fm, T_FIX, 0.1, 0.1)
@@ -127,6 +161,50 @@ def test_extrapolation_is_constant(orc):
     assert orc.eval_spline_3d(grid, Cu, t0, np.nextafter(x1, 2 * x1), y0) == 0.0
     assert orc.eval_spline_3d(grid, Cu, np.nextafter(t0, -1.0), x0, y0) == 0.0
     assert orc.eval_spline_3d(grid, Cu, 0.5 * (t0 + t1), 0.5 * (x0 + x1), y1 + 1.0) == 0.0
+
+
+def _linear_field(a=0.3, bt=-0.7, bx=1.9, by=0.45):
+    """Samples of a field linear in (t, x, y): the natural-boundary cubic
+    spline reproduces it exactly inside the box."""
+    t = np.linspace(0.0, 6.0, 7)
+    x = np.linspace(-2.0, 3.0, 11)
+    y = np.linspace(1.0, 2.5, 6)
+    T, X, Y = np.meshgrid(t, x, y, indexing="ij")
+    return t, x, y, a + bt * T + bx * X + by * Y, (a, bt, bx, by)
+
+
+def test_extrapolation_nearest_and_linear(orc):
+    """extrap_mode "nearest" and "linear" (no reference fixture pins them; the
+    oracle's definition): nearest = the value at the clamped point; linear =
+    that value plus derivative x distance along each clamped axis, which
+    continues a linear field exactly."""
+    t, x, y, U, (a, bt, bx, by) = _linear_field()
+    grid, C, _ = orc.get_interp_arrays_2D(t, x, y, U, U)
+    lin = lambda p: a + bt * p[0] + bx * p[1] + by * p[2]
+    rng = np.random.default_rng(5)
+    inside = np.column_stack([rng.uniform(0, 6, 20), rng.uniform(-2, 3, 20), rng.uniform(1, 2.5, 20)])
+    outside = inside + rng.choice([-1.0, 0.0, 1.0], (20, 3)) * rng.uniform(0.1, 4.0, (20, 3))
+    lo = np.array([0.0, -2.0, 1.0])
+    hi = np.array([6.0, 3.0, 2.5])
+    for p in np.vstack([inside, outside]):
+        c = np.clip(p, lo, hi)
+        v1 = orc.eval_spline_3d(grid, C, *p, extrap=1)
+        assert v1 == orc.eval_spline_3d(grid, C, *c, extrap=1)
+        assert v1 == orc.eval_spline_3d(grid, C, *c, extrap=0)
+        assert abs(v1 - lin(c)) <= 1e-12
+        v2 = orc.eval_spline_3d(grid, C, *p, extrap=2)
+        assert abs(v2 - lin(p)) <= 1e-11, (p, v2, lin(p))
+        if np.any(p != c):
+            assert orc.eval_spline_3d(grid, C, *p, extrap=0) == 0.0
+    # a curved field: "linear" is continuous at the box surface and its slope
+    # beyond it is the one-sided derivative there
+    t, xs, u, v, _ = _spline_case()
+    grid, Cu, _ = orc.get_interp_arrays_2D(t, xs, xs, u, v)
+    edge = orc.eval_spline_3d(grid, Cu, 0.1, 1.0, 0.3, extrap=2)
+    assert orc.eval_spline_3d(grid, Cu, 0.1, 1.0 + 1e-9, 0.3, extrap=2) == pytest.approx(edge, abs=1e-8)
+    d_in = (edge - orc.eval_spline_3d(grid, Cu, 0.1, 1.0 - 1e-6, 0.3)) / 1e-6
+    d_out = (orc.eval_spline_3d(grid, Cu, 0.1, 1.5, 0.3, extrap=2) - edge) / 0.5
+    assert d_out == pytest.approx(d_in, rel=1e-5)
 
 
 GRID_DG = ((0.0, 2.0, 21), (0.0, 1.0, 11))
