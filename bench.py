@@ -76,6 +76,10 @@ def parse():
     ap.add_argument("--learned-full", action="store_true",
                     help="learned proposer: train on seeds 0-7, evaluate seed 8 at 4001x2001 x 96 t0")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the double-gyre (401x201) and precision-sweep legs")
+    ap.add_argument("--learned-t0s", type=int, default=96,
+                    help="held-out learned-proposer evaluation: hourly t0 values from 168 h")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--rtol", type=float, default=None, help="fixed rtol (skips the accuracy ladder)")
     ap.add_argument("--atol", type=float, default=None, help="with --rtol (default 10 rtol)")
@@ -315,16 +319,21 @@ def run_ours(args, rank, world):
                     "lands, and inside the box the error of the most sensitive trajectories "
                     "exceeds the bound at every rtol affordable to either path (ladder: "
                     "max_inside_box)"}
-    # learned step proposer: trained on other flows, used for the headline step
-    # only when it is faster at the same accuracy bound
-    proposer, learned = None, None
+    # learned step proposer: trained on other flows; each proposal mode against
+    # the plain controller on the headline workload, used for the headline
+    # step only when it is faster and meets the same accuracy rule
+    proposer, learned, pmode = None, None, 1
     if prec == "mixed" and not args.quick and not args.no_learned:
         sp, learned = train_proposer(rtol, atol)
-        ms = {}
-        for name, kw in (("mixed", {}), ("mixed+learned", {"step_model": sp, "step_model_mode": 1})):
-            out_ = torch.empty((nx, ny, 2), dtype=torch.float64, device="cuda")
-            nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol, precision="mixed",
-                               out=out_, return_status=True, **kw)
+        box = ((wl["lon"][0], wl["lon"][-1]), (wl["lat"][0], wl["lat"][-1]))
+        modes = {}
+        for name, kw in (("plain", {}),
+                         ("every_step_min", {"step_model": sp, "step_model_mode": 1}),
+                         ("start_and_rejections_min", {"step_model": sp, "step_model_mode": 3}),
+                         ("start_only", {"step_model": sp, "step_model_mode": 4})):
+            out_, _, stl = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol,
+                                              precision="mixed", return_status=True,
+                                              return_stats=True, **kw)
             a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a_.record()
             for _ in range(3):
@@ -332,18 +341,25 @@ def run_ours(args, rank, world):
                                    precision="mixed", out=out_, return_status=True, **kw)
             b_.record()
             torch.cuda.synchronize()
-            ms[name] = a_.elapsed_time(b_) / 3
+            s_ = stl.double()
+            modes[name] = {"mode": kw.get("step_model_mode"), "flowmap_ms": a_.elapsed_time(b_) / 3,
+                           "rhs_evals_per_particle": float(s_[..., 2].mean()),
+                           "rejected_fraction": float(s_[..., 1].sum() /
+                                                      (s_[..., 0] + s_[..., 1]).sum())}
             if truth is not None:
-                learned["error_" + name] = _err_stats(
-                    out_, truth, ((wl["lon"][0], wl["lon"][-1]), (wl["lat"][0], wl["lat"][-1])),
-                    1e-6 * wl["extent"])
-        learned["flowmap_ms"] = ms
-        ok = truth is None or learned["error_mixed+learned"]["q99"] <= 1e-6 * wl["extent"]
-        if ok and ms["mixed+learned"] < ms["mixed"]:
-            proposer = sp
+                e_ = _err_stats(out_, truth, box, 1e-6 * wl["extent"])
+                modes[name].update({"q99": e_["q99"], "mean": e_["mean"]})
+        learned["headline_workload"] = modes
+        best = min((m for m in modes if m != "plain"), key=lambda m: modes[m]["flowmap_ms"])
+        ok = truth is None or modes[best]["q99"] <= 1e-6 * wl["extent"]
+        if ok and modes[best]["flowmap_ms"] < modes["plain"]["flowmap_ms"]:
+            proposer, pmode = sp, modes[best]["mode"]
         learned["used_for_headline"] = proposer is not None
-        learned["heldout"] = run_learned_eval(sp, rtol, atol)
-    mkw = {"step_model": proposer, "step_model_mode": 1} if proposer is not None else {}
+        # the held-out flow (C4): the proposal made only at each particle's
+        # first step (it replaces HINIT) against the plain controller
+        learned["heldout"] = run_learned_eval(
+            sp, rtol, atol, t0s=tuple(168.0 + k for k in range(args.learned_t0s)), mode=4)
+    mkw = {"step_model": proposer, "step_model_mode": pmode} if proposer is not None else {}
 
     # algorithmic step counts from the plain FP64 controller at this rtol
     _, _, st64 = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=rtol, atol=atol,
@@ -487,7 +503,8 @@ def run_ours(args, rank, world):
                    "rtol": rtol, "atol": atol, "l2": "flushed between timed steps",
                    "parallelism": "field per GPU" if world > 1 else "single GPU",
                    "lanes_per_particle": lanes, "blocks_per_sm": bps,
-                   "step_proposer": "learned MLP (min with controller)" if proposer else "dop853 controller"},
+                   "step_proposer": ("learned MLP, step_model_mode %d" % pmode) if proposer
+                   else "dop853 controller"},
         "gpu_launches": int(launches),
         "clocks": ck,
         "roofline": {"bound": "fp32" if prec == "mixed" else "fp64", "achieved": achieved,
@@ -521,7 +538,12 @@ def run_ours(args, rank, world):
     if not args.no_e2e and not args.quick:
         out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
     if not args.no_cpu_baseline and not args.quick and rank == 0:
-        out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value)
+        out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value,
+                                               truth=truth)
+    if not args.quick and not args.no_configs:
+        cpu = rank == 0 and not args.no_cpu_baseline
+        out["c0_double_gyre"] = run_c0(cpu=cpu)
+        out["c3_precision_sweep"] = run_sweep(cpu=cpu)
     return out
 
 
@@ -702,33 +724,34 @@ def run_learned_eval(sp, rtol, atol, nx_ny=(4001, 2001), t0s=(168.0, 192.0, 216.
     return out
 
 
-def run_sweep(oracle_budget_s=60.0):
+def run_sweep(oracle_row_s=2.0, cpu=True):
     """Precision sweep: double gyre 2001x1001 and 4001x2001 (T = -10) and the
     geophysical flow at 0.05 deg (2701x1001, T = -72 h), rtol in {1e-5, 1e-6,
-    1e-8} (atol = 1e-2 rtol): the mixed path against the all-FP64 GPU path and
-    the CPU FP64 oracle (the oracle on every k-th row, all host threads, within
-    a time budget).  Per field: max and mean |mixed - fp64|, |fp64 - oracle|,
-    step counts and times."""
+    1e-8} (atol = 1e-2 rtol): the mixed path against the all-FP64 GPU path
+    (per-field max and mean |mixed - fp64|, step counts, times).  The CPU
+    baseline leg of each row times the C FP64 oracle on a row sample (every
+    k-th row, all host threads, about `oracle_row_s` seconds) and reports both
+    GPU paths' max and mean difference from it there."""
     import torch
     import numbacs_gb300 as nb
-    import oracle
     from numbacs_gb300 import workloads as W
-    oracle.build()
+    if cpu:
+        import oracle
+        oracle.build()
     rows = []
     cases = []
     dg, pdg, _ = nb.get_predefined_flow("double_gyre", int_direction=-1.0)
     for nx, ny in ((2001, 1001), (4001, 2001)):
         x, y = W.double_gyre_grid(nx, ny)
-        cases.append(("double_gyre %dx%d" % (nx, ny), dg, oracle.double_gyre(), 0.0, -10.0, x, y,
-                      pdg, 2.0))
+        cases.append(("double_gyre %dx%d" % (nx, ny), dg, "dg", 0.0, -10.0, x, y, pdg, 2.0))
     wl = geo_setup(180.0)
     lonf, latf = W.geo_ftle_grid(0.05)
     lonf = lonf[lonf <= 35.0 + 1e-9]
-    cases.append(("geo 0.05deg %dx%d" % (len(lonf), len(latf)), wl["flow"],
-                  oracle.spline_flow(wl["grid"], wl["Cu"], wl["Cv"], spherical=1), 180.0, -72.0,
+    cases.append(("geo 0.05deg %dx%d" % (len(lonf), len(latf)), wl["flow"], "geo", 180.0, -72.0,
                   lonf, latf, np.array([-1.0]), wl["extent"]))
-    for name, fl, ofl, t0, T, x, y, p, extent in cases:
+    for name, fl, okind, t0, T, x, y, p, extent in cases:
         xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+        per_row = None
         for rtol in (1e-5, 1e-6, 1e-8):
             atol = 1e-2 * rtol
             res = {}
@@ -744,30 +767,119 @@ def run_sweep(oracle_budget_s=60.0):
                 torch.cuda.synchronize()
                 res[prec] = (fm, st, stats, a.elapsed_time(b))
             d = (res["mixed"][0] - res["fp64"][0]).abs().amax(-1)
-            row = {"field": name, "rtol": rtol, "particles": len(x) * len(y),
+            n = len(x) * len(y)
+            row = {"field": name, "rtol": rtol, "atol": atol, "particles": n, "extent": extent,
                    "mixed_vs_fp64_max": float(d.max()), "mixed_vs_fp64_mean": float(d.mean()),
-                   "extent": extent, "mixed_ms": res["mixed"][3], "fp64_ms": res["fp64"][3],
+                   "mixed_ms": res["mixed"][3], "fp64_ms": res["fp64"][3],
+                   "mixed_particles_per_s": n / (res["mixed"][3] * 1e-3),
+                   "fp64_particles_per_s": n / (res["fp64"][3] * 1e-3),
+                   "speedup": res["fp64"][3] / res["mixed"][3],
                    "mixed_steps": float(res["mixed"][2][..., 0:2].sum(-1).double().mean()),
                    "fp64_steps": float(res["fp64"][2][..., 0:2].sum(-1).double().mean()),
                    "mixed_status_ok": float((res["mixed"][1] == 0).double().mean()),
                    "fp64_status_ok": float((res["fp64"][1] == 0).double().mean())}
-            # CPU FP64 oracle on a row sample sized to the budget
-            stride = max(1, int(len(x) / max(1.0, oracle_budget_s * 8000.0 / len(y))))
-            xs = x[::stride]
-            t_o = time.perf_counter()
-            ofm = oracle.flowmap_grid_2D(ofl, t0, T, xs, y, p, rtol=rtol, atol=atol,
-                                         nthreads=os.cpu_count() or 1)
-            t_o = time.perf_counter() - t_o
-            g = res["fp64"][0][::stride].cpu().numpy()
-            m = res["mixed"][0][::stride].cpu().numpy()
-            eo = np.abs(g - ofm).max(-1)
-            em = np.abs(m - ofm).max(-1)
-            row.update({"oracle_rows_every": stride, "oracle_s": t_o,
-                        "fp64_vs_oracle_max": float(eo.max()), "fp64_vs_oracle_mean": float(eo.mean()),
-                        "mixed_vs_oracle_max": float(em.max()), "mixed_vs_oracle_mean": float(em.mean())})
+            if cpu:
+                ofl = (oracle.double_gyre() if okind == "dg" else
+                       oracle.spline_flow(wl["grid"], wl["Cu"], wl["Cv"], spherical=1))
+                threads = os.cpu_count() or 1
+                if per_row is None:  # calibrate on 2 rows at the tightest tolerance's scale
+                    t_c = time.perf_counter()
+                    oracle.flowmap_grid_2D(ofl, t0, T, x[:: max(1, len(x) // 2)][:2], y, p,
+                                           rtol=1e-8, atol=1e-10, nthreads=threads)
+                    per_row = (time.perf_counter() - t_c) / 2
+                stride = max(1, int(len(x) * per_row / oracle_row_s))
+                xs = x[::stride]
+                t_o = time.perf_counter()
+                ofm = oracle.flowmap_grid_2D(ofl, t0, T, xs, y, p, rtol=rtol, atol=atol,
+                                             nthreads=threads)
+                t_o = time.perf_counter() - t_o
+                g = res["fp64"][0][::stride].cpu().numpy()
+                m = res["mixed"][0][::stride].cpu().numpy()
+                eo = np.abs(g - ofm).max(-1)
+                em = np.abs(m - ofm).max(-1)
+                row["cpu_baseline"] = {
+                    "value": len(xs) * len(y) / t_o, "unit": UNIT, "cores": threads,
+                    "kind": "port", "sample": "every %d-th row (%d particles), %.2f s"
+                                              % (stride, len(xs) * len(y), t_o),
+                    "fp64_gpu_vs_oracle_max": float(eo.max()),
+                    "fp64_gpu_vs_oracle_mean": float(eo.mean()),
+                    "mixed_vs_oracle_max": float(em.max()), "mixed_vs_oracle_mean": float(em.mean())}
             rows.append(row)
             del res
     return rows
+
+
+def run_c0(steps=5, cpu=True):
+    """The reference's own CPU-runnable configuration: double gyre (A = 0.1,
+    eps = 0.25, omega = 2 pi / 10) on a 401 x 201 grid over [0, 2] x [0, 1],
+    t0 = 0, T = -10, DOP853 rtol 1e-6 / atol 1e-8, then ftle_grid_2D
+    (examples/ftle/plot_dg_ftle.py:24-48).  One step = flow map + FTLE of the
+    grid, both paths; errors against the converged FP64 solution (rtol 1e-12);
+    the CPU baseline leg times the C oracle on all host cores and checks the
+    FP64 path against it."""
+    import torch
+    import numbacs_gb300 as nb
+    from numbacs_gb300 import workloads as W
+    fl, p, _ = nb.get_predefined_flow("double_gyre", int_direction=-1.0)
+    x, y = W.double_gyre_grid()
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    T, rtol, atol = -10.0, 1e-6, 1e-8
+    dx, dy = x[1] - x[0], y[1] - y[0]
+    n = len(x) * len(y)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    truth = nb.flowmap_grid_2D(fl, 0.0, T, xd, yd, p, rtol=1e-12, atol=1e-14)
+    out = {"workload": "double gyre 401x201, t0=0, T=-10, rtol 1e-6, atol 1e-8, ftle_grid_2D",
+           "particles": n, "bound": 2e-6}
+    fms = {}
+    for prec in ("mixed", "fp64"):
+        buf = torch.empty((len(x), len(y), 2), dtype=torch.float64, device="cuda")
+        _, st, stats = nb.flowmap_grid_2D(fl, 0.0, T, xd, yd, p, rtol=rtol, atol=atol,
+                                          precision=prec, out=buf, return_status=True,
+                                          return_stats=True)
+        nb.ftle_grid_2D(buf, T, dx, dy)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(steps):
+            flush.zero_()
+            a.record()
+            nb.flowmap_grid_2D(fl, 0.0, T, xd, yd, p, rtol=rtol, atol=atol, precision=prec,
+                               out=buf, return_status=True)
+            nb.ftle_grid_2D(buf, T, dx, dy)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms = sum(ts) / len(ts)
+        s = stats.double()
+        out[prec] = {"ms_per_step": ms, "value": n / (ms * 1e-3),
+                     "rhs_evals_per_particle": float(s[..., 2].mean()),
+                     "rejected_fraction": float(s[..., 1].sum() / (s[..., 0] + s[..., 1]).sum()),
+                     "status_ok": float((st == 0).double().mean()),
+                     "error_vs_converged": _err_stats(buf, truth, ((0.0, 2.0), (0.0, 1.0)), 2e-6)}
+        fms[prec] = buf
+    d = (fms["mixed"] - fms["fp64"]).abs().amax(-1)
+    out["mixed_vs_fp64"] = {"max": float(d.max()), "mean": float(d.mean())}
+    out["speedup_mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    if cpu:
+        import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t = time.perf_counter()
+        ofm, _, ostats = oracle.flowmap_grid_2D(oracle.double_gyre(), 0.0, T, x, y, p, rtol=rtol,
+                                                atol=atol, nthreads=threads, return_status=True)
+        oracle.ftle_grid_2D(ofm, T, dx, dy)
+        secs = time.perf_counter() - t
+        g = fms["fp64"].cpu().numpy()
+        _, _, gst = nb.flowmap_grid_2D(fl, 0.0, T, xd, yd, p, rtol=rtol, atol=atol,
+                                       return_status=True, return_stats=True)
+        out["cpu_baseline"] = {
+            "value": n / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "the whole 401x201 grid, C oracle (OpenMP) flow map + ftle_grid_2D, %.2f s"
+                      % secs,
+            "fp64_gpu_vs_oracle": {"max": float(np.abs(g - ofm).max()),
+                                   "same_step_counts": float(np.all(gst.cpu().numpy() == ostats,
+                                                                    -1).mean())}}
+        out["gpu_over_cpu"] = out["mixed"]["value"] / out["cpu_baseline"]["value"]
+    return out
 
 
 def _profile_traffic(prec):
@@ -985,14 +1097,27 @@ def cpu_sample_rate(wl, rtol, atol, budget_s, threads):
     return 1.0 / per_particle, n_sample, stride, t_fm + t_st, reps
 
 
-def run_cpu_baseline(wl, rtol, atol, budget_s, value_gpu=None):
+def run_cpu_baseline(wl, rtol, atol, budget_s, value_gpu=None, truth=None):
     threads = os.cpu_count() or 1
     rate, n, stride, secs, reps = cpu_sample_rate(wl, rtol, atol, budget_s, threads)
-    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d particles (every %d-th lon row x all 251 lat, %d passes) integrated by "
-                      "the C oracle (DOP853 + tricubic spline, OpenMP) + full-field FTLE/eig/ridge "
-                      "stencils; %.1f s of CPU work; %s" % (n, stride, reps, secs, cpu_model()),
-            "rtol": rtol}
+    out = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "%d particles (every %d-th lon row x all 251 lat, %d passes) integrated by "
+                     "the C oracle (DOP853 + tricubic spline, OpenMP) + full-field FTLE/eig/ridge "
+                     "stencils; %.1f s of CPU work; %s" % (n, stride, reps, secs, cpu_model()),
+           "rtol": rtol, "atol": atol}
+    if truth is not None:
+        # the converged solution the accuracy rules use, from the oracle on
+        # every 16th longitude row
+        import oracle
+        of = oracle.spline_flow(wl["grid"], wl["Cu"], wl["Cv"], spherical=1)
+        t = time.perf_counter()
+        ot = oracle.flowmap_grid_2D(of, wl["t0"], wl["T"], wl["lonf"][::16], wl["latf"],
+                                    wl["params"], rtol=1e-12, atol=1e-14, nthreads=threads)
+        out["truth_check"] = {"rows": "every 16th lon row", "particles": int(ot.shape[0] * ot.shape[1]),
+                              "oracle_s": time.perf_counter() - t,
+                              "max_abs_diff_vs_gpu_truth": float(
+                                  np.abs(ot - truth[::16].cpu().numpy()).max())}
+    return out
 
 
 def run_reference(args, rank, world):

@@ -78,8 +78,12 @@ typedef struct nbcs_opts {
     int32_t threads_per_block; /* FP64 path: 0 = library default (128) */
     int32_t blocks_per_sm;     /* grid cap in blocks per SM; 0 = one block per particle tile */
     int32_t lanes_per_particle; /* mixed spline path: 1, 2 or 4 lanes share a particle; 0 = auto */
-    int32_t step_model_mode;    /* how a step_model proposal h_m meets the controller's h_c:
-                                   0 = h_m, 1 = min(h_m, h_c), 2 = sqrt(h_m h_c) */
+    int32_t step_model_mode;    /* how a step_model proposal h_m meets the controller's h_c.
+                                   At every fresh step: 0 = h_m, 1 = min(h_m, h_c),
+                                   2 = sqrt(h_m h_c).  Only at the first step and after a
+                                   rejection: 3 = min(h_m, h_c); 4 = h_m replaces HINIT's
+                                   initial step (no probe evaluation), then min(h_m, h_c)
+                                   after a rejection */
     int32_t* stats;        /* optional device (n,3) int32: accepted, rejected, RHS evals */
     const void* step_model; /* optional learned step-size proposer (device blob, see nbcs_mlp_*);
                                mixed precision, spline flows */
@@ -230,7 +234,11 @@ int nbcs_ftle_from_eig(const double* eigval, int64_t n, int64_t stride, double T
 
 /* Fused C_eig_2D + ftle_from_eig(eigvals[...,1]) + eigvecs[...,:,1]:
  * flowmap -> ftle (nx,ny) and evec_max (nx,ny,2) in one pass (the inputs of
- * ftle_ridge_pts). */
+ * ftle_ridge_pts).  The scaling divisions (1/(2dx), 1/(2dy), 1/(2|T|)) are
+ * products with reciprocals and the eigenvector is normalised by a reciprocal
+ * square root, so the values are within a few ulp of nbcs_c_eig_2d +
+ * nbcs_ftle_from_eig rather than bit-identical (those two keep the
+ * reference's IEEE divisions). */
 int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, double T, double dx,
                       double dy, const uint8_t* mask, double* ftle, double* evec_max,
                       void* stream);

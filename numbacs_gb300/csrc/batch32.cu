@@ -233,6 +233,10 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         D.den = 2.0 * fabs(F.T);
         D.dx = F.dx;
         D.dy = F.dy;
+        // the fused FTLE stencil's reciprocals, as nbcs_ftle_evec_2d forms them
+        D.rden = 1.0 / (2.0 * fabs(F.T));
+        D.rdx = 1.0 / (2.0 * F.dx);
+        D.rdy = 1.0 / (2.0 * F.dy);
         D.x = F.x;
         D.y = F.y;
         D.mask = F.mask;

@@ -46,6 +46,7 @@ struct DevField {
     int lp, pad_;  // lanes per particle of this field's work units
     double ts, te, rtol, atol;
     double den, dx, dy;  // FTLE: 2|T| and grid spacing
+    double rden, rdx, rdy;  // their reciprocals 1/(2|T|), 1/(2 dx), 1/(2 dy)
     Params P;
     const double* x;
     const double* y;

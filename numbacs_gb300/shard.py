@@ -13,11 +13,20 @@ percentile, and each extracts its rows' ridge points; gathering those in rank
 order gives the single-GPU result bit for bit (row-major order is preserved
 because the blocks are contiguous and in rank order).
 
+Labelled ridges (``ftle_ridges``, ridges.py:186-229) shard the same way:
+each rank labels the ridge mask of its own rows (8-connected), and a
+component that crosses a block boundary is joined on the host: the last
+owned row of rank r and the first of rank r + 1 are neighbours, so their
+labels are united wherever two ridge pixels touch (|dj| <= 1).  Every rank
+gathers the per-rank components (pixel indices and points) and builds the
+same global list: components ordered by their first pixel in row-major order,
+points in row-major order inside each, those with fewer than min_ridge_pts
+points dropped -- the single-GPU result.
+
 The compute goes through an ``ops`` object (flow map, FTLE + eigvec_max,
-percentile, thresholded ridge points): :class:`GpuOps` is the product path;
-a CPU object with the same methods lets the multi-process logic run as gloo
-ranks without GPUs.  Labelled ridges (``ftle_ridges``) are not sharded: a
-component crossing a block boundary needs a merge step that is not built.
+percentile, thresholded ridge points and mask, labels): :class:`GpuOps` is
+the product path; a CPU object with the same methods lets the multi-process
+logic run as gloo ranks without GPUs.
 """
 import numpy as np
 
@@ -61,6 +70,18 @@ class GpuOps:
     def ridge_pts(self, f, evec, x, y, dx, dy, sdd_thresh, f_min):
         from .extraction.ridges import ridge_pts_fmin
         return ridge_pts_fmin(f, evec, x, y, dx, dy, sdd_thresh, f_min)
+
+    def ridge_field(self, f, evec, x, y, dx, dy, sdd_thresh, f_min):
+        """(ridge mask (n, ny) bool, r_pts (n * ny, 2)) with the threshold and
+        spacing given."""
+        from .extraction.ridges import _run
+        _, _, mask, full = _run(f, evec, x, y, sdd_thresh, 0, True, True, f_min=f_min,
+                                dxdy=(dx, dy))
+        return mask.to(bool), full
+
+    def label8(self, mask):
+        from .extraction.ridges import label8
+        return label8(mask)
 
     def to_numpy(self, a):
         return a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
@@ -119,3 +140,95 @@ def sharded_ftle_ridge_pts(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile
     parts = [None] * world
     dist.all_gather_object(parts, pts, group=group)
     return np.concatenate(parts, axis=0)
+
+
+def block_ridges(ops, state, f_global, sdd_thresh=0.0, percentile=0):
+    """Phase 2 of the labelled ridges on one rank: the global threshold, the
+    ridge mask and points of the rank's own rows, their 8-connected labels.
+    Returns {"rows": (i0, i1), "ny", "comps": [(flat pixel indices (global,
+    row-major), points (m, 2))] in local label order, "top", "bottom": the
+    labels of the first and last owned row}."""
+    f_min = 0.0 if percentile == 0 else ops.percentile(f_global, percentile)
+    dx, dy = state["d"]
+    i0, i1, e0, e1 = state["rows"]
+    mask, full = ops.ridge_field(state["f"], state["ev"], state["x"], state["y"], dx, dy,
+                                 sdd_thresh, f_min)
+    ny = len(state["y"])
+    mask = ops.to_numpy(mask)[i0 - e0:i1 - e0]
+    full = ops.to_numpy(full).reshape(e1 - e0, ny, 2)[i0 - e0:i1 - e0]
+    lab, n = ops.label8(np.ascontiguousarray(mask))
+    lab = ops.to_numpy(lab).astype(np.int64)
+    flat = np.arange(i0, i1)[:, None] * ny + np.arange(ny)[None, :]
+    sel = lab.ravel() > 0
+    keys = lab.ravel()[sel]
+    order = np.argsort(keys, kind="stable")  # row-major inside each label
+    idx, pts = flat.ravel()[sel][order], full.reshape(-1, 2)[sel][order]
+    bounds = np.searchsorted(keys[order], np.arange(1, n + 2))
+    comps = [(idx[bounds[k]:bounds[k + 1]], pts[bounds[k]:bounds[k + 1]]) for k in range(n)]
+    return {"rows": (i0, i1), "ny": ny, "comps": comps,
+            "top": lab[0] if i1 > i0 else np.zeros(ny, np.int64),
+            "bottom": lab[-1] if i1 > i0 else np.zeros(ny, np.int64)}
+
+
+def merge_ridges(parts, min_ridge_pts=3):
+    """Join the per-rank components (block_ridges of every rank, in rank
+    order) across block boundaries: the global ftle_ridges list."""
+    offs = np.cumsum([0] + [len(p["comps"]) for p in parts])
+    parent = list(range(int(offs[-1])))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    for r in range(len(parts) - 1):
+        b, t = parts[r]["bottom"], parts[r + 1]["top"]
+        ny = len(b)
+        for j in np.nonzero(b)[0]:
+            for jj in range(max(0, j - 1), min(ny, j + 2)):
+                if t[jj]:
+                    ra, rb = find(offs[r] + b[j] - 1), find(offs[r + 1] + t[jj] - 1)
+                    if ra != rb:
+                        parent[max(ra, rb)] = min(ra, rb)
+    groups = {}
+    for r, p in enumerate(parts):
+        for k, comp in enumerate(p["comps"]):
+            groups.setdefault(find(offs[r] + k), []).append(comp)
+    out = []
+    for members in groups.values():
+        idx = np.concatenate([m[0] for m in members])
+        pts = np.concatenate([m[1] for m in members])
+        o = np.argsort(idx, kind="stable")
+        out.append((idx[o[0]] if len(o) else 0, pts[o]))
+    out.sort(key=lambda c: c[0])
+    return [pts for _, pts in out if len(pts) >= min_ridge_pts]
+
+
+def sharded_ftle_ridges(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile=0,
+                        min_ridge_pts=3, *, group=None, ops=None, **flowmap_kw):
+    """ftle_ridges of the field's flow map (list of (m, 2) numpy arrays),
+    computed by every rank on its row block and joined across the block
+    boundaries; identical on every rank to the one-GPU pipeline
+    flowmap_grid_2D -> ftle_evec_2D -> ftle_ridges.  Collectives: two
+    all_gather_object calls on the host (owned FTLE rows, per-rank
+    components)."""
+    import torch.distributed as dist
+    ops = ops or GpuOps()
+    if dist.is_available() and dist.is_initialized():
+        rank, world = dist.get_rank(group), dist.get_world_size(group)
+    else:
+        rank, world = 0, 1
+    state, owned = block_ftle(ops, rank, world, flow, t0, T, x, y, params, **flowmap_kw)
+    if world == 1:
+        rows = [owned]
+    else:
+        rows = [None] * world
+        dist.all_gather_object(rows, owned, group=group)
+    part = block_ridges(ops, state, np.concatenate(rows, axis=0), sdd_thresh, percentile)
+    if world == 1:
+        parts = [part]
+    else:
+        parts = [None] * world
+        dist.all_gather_object(parts, part, group=group)
+    return merge_ridges(parts, min_ridge_pts)

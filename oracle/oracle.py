@@ -310,6 +310,13 @@ def ftle_ridge_pts(f, eigvec_max, x, y, sdd_thresh=0.0, percentile=0):
     return rpts[mask.ravel()]
 
 
+def ridge_field_fmin(f, eigvec_max, x, y, dx, dy, sdd_thresh, f_min):
+    """(r_pts (nx*ny, 2), ridge mask (nx, ny) bool) with the threshold and the
+    grid spacing given (a row block of a sharded field)."""
+    rpts, mask, _ = _ridge_field(f, eigvec_max, x, y, sdd_thresh, f_min=f_min, dxdy=(dx, dy))
+    return rpts, mask
+
+
 def ridge_pts_fmin(f, eigvec_max, x, y, dx, dy, sdd_thresh, f_min):
     """ftle_ridge_pts with the threshold and the grid spacing given."""
     rpts, mask, _ = _ridge_field(f, eigvec_max, x, y, sdd_thresh, f_min=f_min, dxdy=(dx, dy))
