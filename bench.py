@@ -59,6 +59,28 @@ FLOPS_STEP = 438
 FLOPS_RHS_SPLINE = 330
 
 
+def _jsonable(o):
+    """numpy / torch scalars in the result dict -> Python numbers."""
+    if hasattr(o, "item"):
+        return o.item()
+    if isinstance(o, (set, tuple)):
+        return list(o)
+    raise TypeError("not JSON serialisable: %r" % type(o))
+
+
+_T_START = time.perf_counter()
+
+
+def _leg(name, out=None):
+    """Progress of the run on stderr (leg name and elapsed seconds); with
+    NBCS_BENCH_PARTIAL set, the results so far are also written there."""
+    sys.stderr.write("[bench %7.1f s] %s\n" % (time.perf_counter() - _T_START, name))
+    path = os.environ.get("NBCS_BENCH_PARTIAL")
+    if path and out is not None:
+        with open(path, "w") as fh:
+            json.dump(out, fh, default=_jsonable)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -298,6 +320,7 @@ def run_ours(args, rank, world):
         truth = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=1e-12, atol=1e-14,
                                    return_status=True)[0]
         ladder, rules = accuracy_ladder(nb, wl, x, y, truth)
+        _leg("accuracy ladder")
         head = {p_: next(r for r in ladder if r["precision"] == p_ and r["rtol"] == rtol
                          and r["atol"] == atol) for p_ in ("mixed", "fp64")}
         bound = 1e-6 * wl["extent"]
@@ -355,6 +378,7 @@ def run_ours(args, rank, world):
         if ok and modes[best]["flowmap_ms"] < modes["plain"]["flowmap_ms"]:
             proposer, pmode = sp, modes[best]["mode"]
         learned["used_for_headline"] = proposer is not None
+        _leg("learned proposer modes")
         # the held-out flow (C4): the proposal made only at each particle's
         # first step (it replaces HINIT) against the plain controller
         learned["heldout"] = run_learned_eval(
@@ -531,23 +555,30 @@ def run_ours(args, rank, world):
                        "attempted_steps_fp64": float(att.mean())},
         "plain_fp64": plain,
     }
+    _leg("headline", out)
     if not args.quick and not args.no_batch:
-        out["batch"] = run_batch(wl, rtol, max(2, min(args.steps, 5)))
+        out["batch"] = run_batch(wl, rtol, atol, max(2, min(args.steps, 5)))
+        _leg("batch", out)
     if not args.quick and not args.no_rows:
-        out["composition"], out["aux_grid"], out["ordered_ridges"] = run_rows(wl, rtol)
+        out["composition"], out["aux_grid"], out["ordered_ridges"] = run_rows(wl, rtol, atol)
+        _leg("composition", out)
     if not args.no_e2e and not args.quick:
         out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
+        _leg("e2e", out)
     if not args.no_cpu_baseline and not args.quick and rank == 0:
         out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value,
                                                truth=truth)
+        _leg("cpu_baseline", out)
     if not args.quick and not args.no_configs:
         cpu = rank == 0 and not args.no_cpu_baseline
         out["c0_double_gyre"] = run_c0(cpu=cpu)
+        _leg("c0_double_gyre", out)
         out["c3_precision_sweep"] = run_sweep(cpu=cpu)
+        _leg("c3_precision_sweep", out)
     return out
 
 
-def run_batch(wl, rtol, steps):
+def run_batch(wl, rtol, atol, steps):
     """Batched time series: 48 geophysical fields (t0 = 168 + k h, T ~ U[-120, -24] h,
     spacing in {0.1, 0.2, 0.4} deg) plus the Bickley jet on 1001 x 301 for 40 days, all
     in one launch replayed from a CUDA graph (schedule autotuned: persistent
@@ -557,7 +588,6 @@ def run_batch(wl, rtol, steps):
     import numbacs_gb300 as nb
     from numbacs_gb300 import workloads as W
     from numbacs_gb300.batch import Field, FTLEBatch
-    atol = 1e-2 * rtol
     fields = []
     for t0, T, sp in W.geo_batch_specs(seed=1):
         lonf, latf = W.geo_ftle_grid(sp)
@@ -903,7 +933,7 @@ def _hbm_peak():
         return None
 
 
-def run_rows(wl, rtol, nT=72):
+def run_rows(wl, rtol, atol, nT=72):
     """Flow-map composition, the auxiliary grid and ordered ridges on the
     headline workload.
 
@@ -923,7 +953,7 @@ def run_rows(wl, rtol, nT=72):
     fms = torch.empty((nT, nx, ny, 2), dtype=torch.float64, device="cuda")
     t = wl["t0"]
     for k in range(nT):
-        nb.flowmap_grid_2D(wl["flow"], t, -1.0, x, y, wl["params"], rtol=rtol, atol=1e-2 * rtol,
+        nb.flowmap_grid_2D(wl["flow"], t, -1.0, x, y, wl["params"], rtol=rtol, atol=atol,
                            precision="mixed", out=fms[k])
         t -= 1.0
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -943,11 +973,11 @@ def run_rows(wl, rtol, nT=72):
     # flowmap_composition_initial: the nT one-hour integrations (parallel
     # streams) and the composition, as a time series starts
     nb.flowmap_composition_initial(wl["flow"], wl["t0"], -float(nT), -1.0, x, y, grid,
-                                   wl["params"], rtol=rtol, atol=1e-2 * rtol, precision="mixed")
+                                   wl["params"], rtol=rtol, atol=atol, precision="mixed")
     torch.cuda.synchronize()
     a.record()
     nb.flowmap_composition_initial(wl["flow"], wl["t0"], -float(nT), -1.0, x, y, grid,
-                                   wl["params"], rtol=rtol, atol=1e-2 * rtol, precision="mixed")
+                                   wl["params"], rtol=rtol, atol=atol, precision="mixed")
     b.record()
     torch.cuda.synchronize()
     ms_init = a.elapsed_time(b)
@@ -959,11 +989,11 @@ def run_rows(wl, rtol, nT=72):
             "note": "gathers of neighbouring particles share sectors: DRAM traffic is below the "
                     "algorithmic bytes"}
     fa = nb.flowmap_aux_grid_2D(wl["flow"], wl["t0"], wl["T"], x, y, wl["params"], rtol=rtol,
-                                atol=1e-2 * rtol)
+                                atol=atol)
     torch.cuda.synchronize()
     a.record()
     fa = nb.flowmap_aux_grid_2D(wl["flow"], wl["t0"], wl["T"], x, y, wl["params"], rtol=rtol,
-                                atol=1e-2 * rtol)
+                                atol=atol)
     b.record()
     torch.cuda.synchronize()
     ms_aux = a.elapsed_time(b)
@@ -1134,10 +1164,12 @@ def run_reference(args, rank, world):
     wl = dict(grid=grid, Cu=Cu, Cv=Cv, lonf=lonf, latf=latf, t0=180.0, T=W.GEO_T,
               pct=W.GEO_PERCENTILE, params=np.array([-1.0]), dx=lonf[1] - lonf[0],
               dy=latf[1] - latf[0])
-    # the tolerance the accuracy ladder selects for the FP64 path on this
-    # workload (the loosest rtol within the flow-map error bound)
-    rtol = args.rtol or 1e-7
-    atol = 1e-2 * rtol
+    # the headline tolerance of the GPU arm (the same configuration)
+    if args.rtol:
+        rtol = args.rtol
+        atol = args.atol if args.atol is not None else 10.0 * rtol
+    else:
+        rtol, atol = HEADLINE_RTOL, HEADLINE_ATOL
     budget = max(2.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         cpu_sample_rate(wl, rtol, atol, budget, os.cpu_count())
@@ -1273,11 +1305,12 @@ def main():
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:
             return 0
-        print(json.dumps(run_reference(args, 0, int(os.environ.get("WORLD_SIZE", "1")))))
+        print(json.dumps(run_reference(args, 0, int(os.environ.get("WORLD_SIZE", "1"))),
+                         default=_jsonable))
         return 0
     if args.sweep:
         dist_setup()
-        print(json.dumps({"precision_sweep": run_sweep()}))
+        print(json.dumps({"precision_sweep": run_sweep()}, default=_jsonable))
         return 0
     if args.learned_full:
         dist_setup()
@@ -1285,12 +1318,12 @@ def main():
         sp, info = train_proposer(wl_rtol, 1e-2 * wl_rtol)
         t0s = tuple(168.0 + k for k in range(96))
         info["heldout"] = run_learned_eval(sp, wl_rtol, 1e-2 * wl_rtol, t0s=t0s)
-        print(json.dumps({"learned_full": info}))
+        print(json.dumps({"learned_full": info}, default=_jsonable))
         return 0
     rank, world, _ = dist_setup()
     out = run_ours(args, rank, world)
     if rank == 0:
-        print(json.dumps(out))
+        print(json.dumps(out, default=_jsonable))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

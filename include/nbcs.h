@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define NBCS_ABI_VERSION 2
+#define NBCS_ABI_VERSION 3
 
 /* return codes */
 #define NBCS_OK 0
@@ -179,6 +179,19 @@ typedef struct nbcs_field {
     double* evec_max;    /* (nx, ny, 2); used when ftle != NULL */
 } nbcs_field;
 
+/* The fields of a batch that share one integrator instantiation (flow kind;
+ * for spline flows also the spherical mode and whether the grid nodes are
+ * floats): one launch of the class's tile kernel integrates all of them. */
+#define NBCS_BATCH_MAX_CLASSES 8
+typedef struct nbcs_batch_class {
+    int32_t kind, spherical, exact_nodes, lanes; /* lanes per particle */
+    int32_t field0, nfields;  /* a contiguous range of the plan's field table */
+    int64_t tiles;            /* 256-thread particle tiles of the class's fields */
+    int32_t flow, reserved;   /* the flow every field of the class uses, else -1 */
+    double r, grid[9];        /* that flow's radius and spline grid (kernel arguments) */
+    const float* coef_uv32;   /* and its FP32 coefficients */
+} nbcs_batch_class;
+
 /* Host-side handle of a prepared batch (filled by nbcs_batch_prepare). */
 typedef struct nbcs_batch {
     void* scratch;       /* device memory holding the batch description */
@@ -186,6 +199,8 @@ typedef struct nbcs_batch {
     int64_t total_chunks; /* 32-particle work units over all fields */
     int64_t ftle_blocks;  /* 256-point FTLE work units */
     int64_t tiles;        /* particle tiles of one 256-thread block over all fields */
+    int32_t nclasses, reserved2;
+    nbcs_batch_class classes[NBCS_BATCH_MAX_CLASSES];
 } nbcs_batch;
 
 size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields);
@@ -194,17 +209,27 @@ size_t nbcs_batch_scratch_bytes(int32_t nflows, int32_t nfields);
 int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const nbcs_field* fields,
                        int32_t nfields, int32_t precision, void* scratch, size_t scratch_bytes,
                        nbcs_batch* plan, void* stream);
-/* Integrate every particle of every field in one launch, then run the
- * FTLE/eigvec stencil of all fields in one launch.  Kernel launches only:
- * capturable in a CUDA graph.  Two schedules, chosen by opts->blocks_per_sm:
- *   >= 0  persistent grid of blocks_per_sm blocks per SM (0 = full occupancy)
- *         whose warps take 32-particle chunks from a shared counter;
- *   <  0  (mixed precision) one block per particle tile of any field, the
- *         hardware block scheduler balancing the tiles of all fields.
+/* Integrate every particle of every field, then run the FTLE/eigvec stencil
+ * of all fields in one launch.  Kernel launches only: capturable in a CUDA
+ * graph.  Two schedules, chosen by opts->blocks_per_sm:
+ *   >= 0  one persistent grid of blocks_per_sm blocks per SM (0 = full
+ *         occupancy) whose warps take 32-particle chunks of any field from a
+ *         shared counter;
+ *   <  0  (mixed precision) per flow class one launch of that class's tile
+ *         kernel -- the single-field integrator's block shape and register
+ *         budget -- with one block per particle tile of the class's fields,
+ *         fields ordered longest first (|T|, then size), the hardware block
+ *         scheduler balancing the tiles; the classes run one after another
+ *         on `stream` (nbcs_batch_run_class launches one class, so a caller
+ *         can put the classes on parallel streams).
  * Either way fields of different sizes and lengths share the GPU instead of
  * each leaving it idle at the end of its own launch.  opts: precision is
  * taken from the plan; stats/step_model unused. */
 int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, void* stream);
+/* The tile kernel of class k of a mixed-precision plan (no FTLE). */
+int nbcs_batch_run_class(const nbcs_batch* plan, int32_t k, const nbcs_opts* opts, void* stream);
+/* The FTLE/eigvec stencil of every field of the plan (after its flow maps). */
+int nbcs_batch_run_ftle(const nbcs_batch* plan, void* stream);
 
 /* ------------------------------------------------------------ diagnostics */
 

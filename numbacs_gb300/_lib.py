@@ -45,12 +45,27 @@ class NbcsField(ctypes.Structure):
                 ("ftle", ctypes.c_void_p), ("evec_max", ctypes.c_void_p)]
 
 
+BATCH_MAX_CLASSES = 8
+
+
+class NbcsBatchClass(ctypes.Structure):
+    """Mirror of ``struct nbcs_batch_class``."""
+    _fields_ = [("kind", ctypes.c_int32), ("spherical", ctypes.c_int32),
+                ("exact_nodes", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("field0", ctypes.c_int32), ("nfields", ctypes.c_int32),
+                ("tiles", ctypes.c_int64), ("flow", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("r", ctypes.c_double), ("grid", ctypes.c_double * 9),
+                ("coef_uv32", ctypes.c_void_p)]
+
+
 class NbcsBatch(ctypes.Structure):
     """Mirror of ``struct nbcs_batch``."""
     _fields_ = [("scratch", ctypes.c_void_p), ("nflows", ctypes.c_int32),
                 ("nfields", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("total_chunks", ctypes.c_int64),
-                ("ftle_blocks", ctypes.c_int64), ("tiles", ctypes.c_int64)]
+                ("ftle_blocks", ctypes.c_int64), ("tiles", ctypes.c_int64),
+                ("nclasses", ctypes.c_int32), ("reserved2", ctypes.c_int32),
+                ("classes", NbcsBatchClass * BATCH_MAX_CLASSES)]
 
 
 # name -> (restype, argtypes)
@@ -99,6 +114,9 @@ SIGNATURES = {
     "nbcs_batch_prepare": (ctypes.c_int, [_FP, _i32, ctypes.POINTER(NbcsField), _i32, _i32, _vp,
                                           _sz, ctypes.POINTER(NbcsBatch), _vp]),
     "nbcs_batch_run": (ctypes.c_int, [ctypes.POINTER(NbcsBatch), ctypes.POINTER(NbcsOpts), _vp]),
+    "nbcs_batch_run_class": (ctypes.c_int, [ctypes.POINTER(NbcsBatch), _i32,
+                                            ctypes.POINTER(NbcsOpts), _vp]),
+    "nbcs_batch_run_ftle": (ctypes.c_int, [ctypes.POINTER(NbcsBatch), _vp]),
     "nbcs_ridge_noalloc_scratch_bytes": (_sz, []),
     "nbcs_ridge_pts_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp,
                                               _vp, _vp, _vp]),

@@ -6,13 +6,16 @@ The reference builds FTLE time series with a Python loop over t0 that calls
 examples/time_series/plot_dg_numbacs_vs_scipy.py).  :class:`FTLEBatch` takes
 the whole list of fields -- any mix of flows, start times, integration
 lengths and grid sizes -- and runs them under one of three schedules: one
-persistent kernel whose warps take 32-particle chunks from a shared counter,
-or one kernel with one block per particle tile of any field (csrc/batch32.cu,
-csrc/batch64.cu), each followed by one FTLE/eigenvector launch for all
-fields; or every field's own single-field integrator and FTLE launches spread
-over parallel streams, longest first, so that the tail of one field overlaps
-the start of the next.  The run is kernel launches only, so it is captured
-once in a CUDA graph and replayed.
+persistent kernel whose warps take 32-particle chunks from a shared counter
+(csrc/batch32.cu, csrc/batch64.cu); or per flow class (the fields that share
+one right-hand side) one launch of a tile kernel with the single-field
+integrator's block shape and register budget, one block per particle tile of
+the class's fields, longest fields first, the classes on parallel streams;
+each followed by one FTLE/eigenvector launch for all fields; or every field's
+own single-field integrator and FTLE launches spread over parallel streams,
+longest first, so that the tail of one field overlaps the start of the next.
+The run is kernel launches only, so it is captured once in a CUDA graph and
+replayed.
 """
 import ctypes
 
@@ -55,6 +58,7 @@ class Field:
         return self.x.numel() * self.y.numel()
 
 
+TILES = -1    # schedule: per flow class one tile kernel (classes on parallel streams)
 STREAMS = -2  # schedule: one integrator + one FTLE launch per field on parallel streams
 
 
@@ -63,8 +67,10 @@ class FTLEBatch:
 
     ``precision`` is "mixed" or "fp64"; ``blocks_per_sm`` picks the schedule:
     >= 0 a persistent grid of that many blocks per SM (0: full occupancy) whose
-    warps take particle chunks from a shared counter, -1 (mixed) one block per
-    particle tile of any field, -2 (``STREAMS``) each field's own single-field
+    warps take particle chunks from a shared counter, -1 (``TILES``, mixed)
+    per flow class one launch of the single-field integrator's block shape
+    over the tiles of the class's fields, longest field first, the classes on
+    parallel streams, -2 (``STREAMS``) each field's own single-field
     integrator and FTLE launches, spread longest first over ``max_streams``
     streams so that one field's tail overlaps the next field's start; None
     takes it from the autotuner cache, tuning on first use.  ``graph=True``
@@ -125,6 +131,7 @@ class FTLEBatch:
         self.max_steps = int(max_steps)
         self.max_streams = max(1, int(max_streams))
         self._streams = None
+        self._class_streams = None
         # longest work first: particles x |T|
         self._order = sorted(range(len(self.fields)),
                              key=lambda k: -self.fields[k].particles * abs(self.fields[k].T))
@@ -152,8 +159,29 @@ class FTLEBatch:
         if bps == STREAMS:
             self._launch_streams()
             return
+        if bps == TILES and self.precision == "mixed" and self.plan.nclasses > 1:
+            self._launch_classes()
+            return
         _lib.check(_lib.load().nbcs_batch_run(ctypes.byref(self.plan), self._opts(blocks_per_sm),
                                               D.stream_ptr()))
+
+    def _launch_classes(self):
+        """The tile kernel of each flow class on its own stream (forked from and
+        joined back into the current stream, capturable), then one FTLE launch
+        for every field."""
+        L = _lib.load()
+        main = torch.cuda.current_stream()
+        n = self.plan.nclasses
+        if self._class_streams is None:
+            self._class_streams = [torch.cuda.Stream() for _ in range(n)]
+        o = self._opts(TILES)
+        for k, s in enumerate(self._class_streams):
+            s.wait_stream(main)
+            _lib.check(L.nbcs_batch_run_class(ctypes.byref(self.plan), k, o,
+                                              ctypes.c_void_p(s.cuda_stream)))
+        for s in self._class_streams:
+            main.wait_stream(s)
+        _lib.check(L.nbcs_batch_run_ftle(ctypes.byref(self.plan), D.stream_ptr()))
 
     def _launch_streams(self):
         """Every field through the single-field entry points (nbcs_flowmap_grid_2d,

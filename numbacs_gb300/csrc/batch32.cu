@@ -10,6 +10,7 @@
 // leaving SMs idle at the end of a per-field launch.  The counter is reset by
 // a one-thread kernel at the start of every run, so a run is two or three
 // kernel launches and can be captured in a CUDA graph.
+#include <algorithm>
 #include <vector>
 
 #include "batch_common.cuh"
@@ -97,29 +98,107 @@ batch32_kernel(BatchHeader* hdr, const DevFlow32* __restrict__ flows,
     }
 }
 
-// tile schedule: block b integrates block tile b of the concatenated fields
-// (the single-field kernel's block size, tiles and warp sub-tiles: 16 x 8
-// particles per block at two lanes a particle); the hardware block scheduler
-// starts a new tile wherever one finishes.  One kernel holds every flow kind,
-// which takes 128 registers a thread without spills: 2 resident blocks (16
-// geophysical fields at 0.4 deg: 22.2 ms; 128-thread blocks 22.4 ms; a
-// 3-block bound spills and takes 24.5 ms).
-constexpr int kBatchTileThreads = 256;
-constexpr int kBatchTileMinBlocks = 2;
+// Tile schedule, one launch per flow class: block b integrates tile b of the
+// class's fields (field table ordered longest first), with the single-field
+// integrator's block (256 threads), tile map (16 x 8 particles at two lanes
+// a particle, 32 x 8 at one) and register budget (3 resident blocks).  The
+// kernel is instantiated for one right-hand side, so it keeps the
+// single-field kernel's 80 registers where one kernel for every flow kind
+// took 128 (2 blocks per SM); each particle's arithmetic is the single-field
+// kernel's, so the results are bit-identical to it.
+// The right-hand side of a field: the kernel argument when every field of the
+// class uses one flow (UNIFORM: the single-field kernel's form, read from the
+// constant bank), else rebuilt from the flow table.
+template <class Flow>
+struct FlowFromDev {
+    __device__ static Flow make(const DevFlow32&) { return Flow{}; }
+};
+template <int SPH, int LP, bool EX>
+struct FlowFromDev<FlowSpline32<SPH, LP, EX>> {
+    __device__ static FlowSpline32<SPH, LP, EX> make(const DevFlow32& f)
+    {
+        return FlowSpline32<SPH, LP, EX>{f.g, f.c, f.deg_per_km};
+    }
+};
 
-__global__ void __launch_bounds__(kBatchTileThreads, kBatchTileMinBlocks)
-batch32_tiles_kernel(const DevFlow32* __restrict__ flows, const DevField* __restrict__ fields,
-                     int nfields, int nmax)
+template <class Flow, bool UNIFORM>
+__global__ void __launch_bounds__(kFm32Block, kFm32MinBlocks)
+batch32_class_kernel(Flow fl0, const DevFlow32* __restrict__ flows,
+                     const DevField* __restrict__ fields, int nfields, int nmax)
 {
-    __shared__ float2 ks[12 * kBatchTileThreads];
-    float2* kc = ks + threadIdx.x;
+    constexpr int LP = Flow::LP;
+    constexpr int KS = kFm32Block / LP;  // one stage column per particle, shared by its lanes
+    __shared__ float2 ks[12 * KS];
+    __shared__ ParamsF sP;  // the block's field is uniform: its parameters once per block
+    float2* kc = ks + threadIdx.x / LP;
     const long long b = blockIdx.x;
     const DevField& F = fields[batch_find<kByTile>(fields, nfields, b)];
-    const long t = (long)(b - F.tile0) * kBatchTileThreads + threadIdx.x;
+    if (threadIdx.x < NBCS_MAX_PARAMS) sP.v[threadIdx.x] = (float)F.P.v[threadIdx.x];
+    __syncthreads();
+    const long t = (long)(b - F.tile0) * kFm32Block + threadIdx.x;
     int i, j;
-    const bool ok = F.lp == 2 ? tile_particle<2, kBatchTileThreads>(t, F.nx, F.ny, &i, &j)
-                              : tile_particle<1, kBatchTileThreads>(t, F.nx, F.ny, &i, &j);
-    if (ok) batch_solve32<kBatchTileThreads>(flows, F, i, j, threadIdx.x & 31, kc, nmax);
+    // the lanes of a group share the particle: they leave together
+    if (!tile_particle<LP, kFm32Block, kFm32TileJ>(t, F.nx, F.ny, &i, &j)) return;
+    const long p = (long)i * F.ny + j;
+    double r0 = 0.0, r1 = 0.0;
+    int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
+    if (!(F.mask && F.mask[p])) {
+        F2 yv[2] = {f2_from_double(F.x[i]), f2_from_double(F.y[j])};
+        st = dop853_solve32<Flow, KS>(UNIFORM ? fl0 : FlowFromDev<Flow>::make(flows[F.flow]), sP,
+                                      f2_from_double(F.ts), f2_from_double(F.te), yv,
+                                      (float)F.rtol, (float)F.atol, nmax, kc, &a, &rj, &nf);
+        r0 = f2_to_double(yv[0]);
+        r1 = f2_to_double(yv[1]);
+    }
+    if (LP == 1 || (threadIdx.x & (LP - 1)) == 0) {
+        reinterpret_cast<double2*>(F.out)[p] = make_double2(r0, r1);
+        if (F.status) F.status[p] = st;
+    }
+}
+
+template <class Flow>
+static int launch_class(const nbcs_batch_class& c, const Flow& fl, const DevFlow32* flows,
+                        const DevField* fields, int nmax, cudaStream_t s)
+{
+    if (c.flow >= 0)
+        batch32_class_kernel<Flow, true><<<(unsigned)c.tiles, kFm32Block, 0, s>>>(
+            fl, flows, fields + c.field0, c.nfields, nmax);
+    else
+        batch32_class_kernel<Flow, false><<<(unsigned)c.tiles, kFm32Block, 0, s>>>(
+            fl, flows, fields + c.field0, c.nfields, nmax);
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+template <int SPH, bool EX>
+static int launch_spline_class(const nbcs_batch_class& c, const DevFlow32* flows,
+                               const DevField* fields, int nmax, cudaStream_t s)
+{
+    FlowSpline32<SPH, 2, EX> fl{};
+    if (c.flow >= 0)
+        fl = FlowSpline32<SPH, 2, EX>{make_grid_f(c.grid), c.coef_uv32,
+                                      (float)(180.0 / (3.141592653589793 * c.r))};
+    return launch_class(c, fl, flows, fields, nmax, s);
+}
+
+int launch_batch32_class(const nbcs_batch_class& c, const DevFlow32* flows,
+                         const DevField* fields, int nmax, cudaStream_t s)
+{
+    if (c.tiles <= 0) return NBCS_OK;
+    if (c.tiles > 0x7fffffffLL) return set_error(NBCS_ERR_UNSUPPORTED, "batch: too many tiles");
+    switch (c.kind) {
+    case NBCS_FLOW_DOUBLE_GYRE: return launch_class(c, FlowDG32{}, flows, fields, nmax, s);
+    case NBCS_FLOW_BICKLEY: return launch_class(c, FlowBickley32{}, flows, fields, nmax, s);
+    default:
+        switch (c.spherical * 2 + (c.exact_nodes ? 1 : 0)) {
+        case 1: return launch_spline_class<0, true>(c, flows, fields, nmax, s);
+        case 2: return launch_spline_class<1, false>(c, flows, fields, nmax, s);
+        case 3: return launch_spline_class<1, true>(c, flows, fields, nmax, s);
+        case 4: return launch_spline_class<2, false>(c, flows, fields, nmax, s);
+        case 5: return launch_spline_class<2, true>(c, flows, fields, nmax, s);
+        default: return launch_spline_class<0, false>(c, flows, fields, nmax, s);
+        }
+    }
 }
 
 static int persistent_blocks(const void* kernel, int threads, int blocks_per_sm)
@@ -141,16 +220,6 @@ int launch_batch32(const BatchHeader* dev_hdr, const DevFlow32* flows, const Dev
     NBCS_LAUNCH_CHECK();
     int blocks = persistent_blocks((const void*)batch32_kernel, kBatchThreads, blocks_per_sm);
     batch32_kernel<<<blocks, kBatchThreads, 0, s>>>(hdr, flows, fields, nfields, nmax);
-    NBCS_LAUNCH_CHECK();
-    return NBCS_OK;
-}
-
-int launch_batch32_tiles(const DevFlow32* flows, const DevField* fields, int nfields,
-                         long long tiles, int nmax, cudaStream_t s)
-{
-    if (tiles > 0x7fffffffLL) return set_error(NBCS_ERR_UNSUPPORTED, "batch: too many tiles");
-    batch32_tiles_kernel<<<(unsigned)tiles, kBatchTileThreads, 0, s>>>(flows, fields, nfields,
-                                                                       nmax);
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
@@ -201,7 +270,12 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         f32[k].deg_per_km = (float)(180.0 / (3.141592653589793 * fl.r));
         f64[k].r = fl.r;
     }
-    long long chunks = 0, blocks = 0, tiles = 0;
+    // validate, then classify: fields that share one integrator
+    // instantiation (flow kind; for splines the spherical mode and float
+    // nodes) form a class, launched as one tile kernel
+    std::vector<int> cls(nfields);
+    int nclasses = 0;
+    nbcs_batch_class classes[NBCS_BATCH_MAX_CLASSES] = {};
     for (int k = 0; k < nfields; ++k) {
         const nbcs_field& F = fields[k];
         if (F.flow < 0 || F.flow >= nflows)
@@ -220,6 +294,51 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
             return set_error(NBCS_ERR_INVALID, "batch field %d: outputs must be 16-byte aligned", k);
         if (F.ftle && !F.evec_max)
             return set_error(NBCS_ERR_INVALID, "batch field %d: ftle needs evec_max", k);
+        const nbcs_flow& fl = flows[F.flow];
+        const bool spline = fl.kind == NBCS_FLOW_SPLINE2D;
+        nbcs_batch_class key = {};
+        key.kind = fl.kind;
+        key.spherical = spline ? fl.spherical : 0;
+        key.exact_nodes = spline && grid_nodes_exact_f(fl.grid) ? 1 : 0;
+        key.lanes = (precision == NBCS_PREC_MIXED && spline) ? 2 : 1;
+        int c = 0;
+        while (c < nclasses && !(classes[c].kind == key.kind &&
+                                 classes[c].spherical == key.spherical &&
+                                 classes[c].exact_nodes == key.exact_nodes))
+            ++c;
+        if (c == nclasses) {
+            if (nclasses == NBCS_BATCH_MAX_CLASSES)
+                return set_error(NBCS_ERR_UNSUPPORTED, "batch: more than %d flow classes",
+                                 NBCS_BATCH_MAX_CLASSES);
+            key.flow = F.flow;
+            key.r = fl.r;
+            for (int q = 0; q < 9; ++q) key.grid[q] = fl.grid[q];
+            key.coef_uv32 = fl.coef_uv32;
+            classes[nclasses++] = key;
+        } else if (classes[c].flow != F.flow) {
+            classes[c].flow = -1;  // fields of several flows: each block reads its own
+        }
+        cls[k] = c;
+    }
+    // field table order: by class, then longest first (|T|, then particles),
+    // so each class's tiles run longest first and the last tiles are short
+    std::vector<int> order(nfields);
+    for (int k = 0; k < nfields; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
+        if (cls[p] != cls[q]) return cls[p] < cls[q];
+        const double tp = fabs(fields[p].T), tq = fabs(fields[q].T);
+        if (tp != tq) return tp > tq;
+        return (long)fields[p].nx * fields[p].ny > (long)fields[q].nx * fields[q].ny;
+    });
+    long long chunks = 0, blocks = 0, tiles = 0, class_tiles = 0;
+    for (int k = 0; k < nfields; ++k) {
+        const nbcs_field& F = fields[order[k]];
+        nbcs_batch_class& C = classes[cls[order[k]]];
+        if (C.nfields == 0) {  // classes are contiguous in `order`
+            C.field0 = k;
+            class_tiles = 0;
+        }
+        C.nfields++;
         DevField& D = df[k];
         D.flow = F.flow;
         D.nx = F.nx;
@@ -244,18 +363,21 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
         D.status = F.status;
         D.ftle = F.ftle;
         D.evec = F.evec_max;
-        D.lp = (precision == NBCS_PREC_MIXED && flows[F.flow].kind == NBCS_FLOW_SPLINE2D) ? 2 : 1;
+        D.lp = C.lanes;
         D.chunk0 = chunks;
         D.block0 = blocks;
-        D.tile0 = tiles;
+        D.tile0 = class_tiles;  // tiles are counted within the class
         long n = (long)F.nx * F.ny;
         const int tj = batch_tile_j(D.lp);
         chunks += (long long)((F.nx + kBatchTileI - 1) / kBatchTileI) * ((F.ny + tj - 1) / tj);
         if (F.ftle) blocks += (n + kFtleBlock - 1) / kFtleBlock;
-        // block tile of the tile schedule: (ti x tj) particles
-        const int ti = D.lp == 2 ? TileShape<2, kBatchTileThreads>::TI : TileShape<1, kBatchTileThreads>::TI;
-        const int tjt = D.lp == 2 ? TileShape<2, kBatchTileThreads>::TJ : TileShape<1, kBatchTileThreads>::TJ;
-        tiles += (long long)((F.nx + ti - 1) / ti) * ((F.ny + tjt - 1) / tjt);
+        // block tile of the class kernels: (ti x tj) particles
+        const int ti = D.lp == 2 ? TileShape<2, kFm32Block>::TI : TileShape<1, kFm32Block>::TI;
+        const int tjt = D.lp == 2 ? TileShape<2, kFm32Block>::TJ : TileShape<1, kFm32Block>::TJ;
+        const long long ft = (long long)((F.nx + ti - 1) / ti) * ((F.ny + tjt - 1) / tjt);
+        class_tiles += ft;
+        C.tiles += ft;
+        tiles += ft;
     }
     hdr->counter = 0;
     hdr->total_chunks = chunks;
@@ -272,7 +394,43 @@ extern "C" int nbcs_batch_prepare(const nbcs_flow* flows, int32_t nflows, const 
     plan->total_chunks = chunks;
     plan->ftle_blocks = blocks;
     plan->tiles = tiles;
+    plan->nclasses = nclasses;
+    plan->reserved2 = 0;
+    for (int c = 0; c < NBCS_BATCH_MAX_CLASSES; ++c)
+        plan->classes[c] = c < nclasses ? classes[c] : nbcs_batch_class{};
     return NBCS_OK;
+}
+
+static const DevField* plan_fields(const nbcs_batch* plan)
+{
+    const BatchLayout lay = batch_layout(plan->nflows, plan->nfields);
+    return reinterpret_cast<const DevField*>(static_cast<unsigned char*>(plan->scratch) +
+                                             lay.off_fields);
+}
+
+extern "C" int nbcs_batch_run_class(const nbcs_batch* plan, int32_t k, const nbcs_opts* opts,
+                                    void* stream)
+{
+    NBCS_RANGE();
+    if (!plan || !plan->scratch) return set_error(NBCS_ERR_INVALID, "batch_run_class: no plan");
+    if (plan->precision != NBCS_PREC_MIXED)
+        return set_error(NBCS_ERR_UNSUPPORTED, "batch_run_class: mixed-precision plans only");
+    if (k < 0 || k >= plan->nclasses)
+        return set_error(NBCS_ERR_INVALID, "batch_run_class: class %d of %d", k, plan->nclasses);
+    const BatchLayout lay = batch_layout(plan->nflows, plan->nfields);
+    const DevFlow32* f32 = reinterpret_cast<const DevFlow32*>(
+        static_cast<unsigned char*>(plan->scratch) + lay.off_f32);
+    const int nmax = (opts && opts->max_steps > 0) ? opts->max_steps : 100000;
+    return launch_batch32_class(plan->classes[k], f32, plan_fields(plan), nmax, as_stream(stream));
+}
+
+extern "C" int nbcs_batch_run_ftle(const nbcs_batch* plan, void* stream)
+{
+    NBCS_RANGE();
+    if (!plan || !plan->scratch) return set_error(NBCS_ERR_INVALID, "batch_run_ftle: no plan");
+    if (plan->ftle_blocks <= 0) return NBCS_OK;
+    return launch_ftle_batch(plan_fields(plan), plan->nfields, plan->ftle_blocks,
+                             as_stream(stream));
 }
 
 extern "C" int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, void* stream)
@@ -282,20 +440,25 @@ extern "C" int nbcs_batch_run(const nbcs_batch* plan, const nbcs_opts* opts, voi
     const BatchLayout lay = batch_layout(plan->nflows, plan->nfields);
     unsigned char* base = static_cast<unsigned char*>(plan->scratch);
     const BatchHeader* hdr = reinterpret_cast<const BatchHeader*>(base);
-    const DevField* fields = reinterpret_cast<const DevField*>(base + lay.off_fields);
+    const DevField* fields = plan_fields(plan);
     const int bps = opts ? opts->blocks_per_sm : 0;
     const int nmax = (opts && opts->max_steps > 0) ? opts->max_steps : 100000;
     cudaStream_t s = as_stream(stream);
     int rc;
     if (plan->total_chunks > 0) {
         const DevFlow32* f32 = reinterpret_cast<const DevFlow32*>(base + lay.off_f32);
-        if (plan->precision == NBCS_PREC_MIXED && bps < 0)
-            rc = launch_batch32_tiles(f32, fields, plan->nfields, plan->tiles, nmax, s);
-        else if (plan->precision == NBCS_PREC_MIXED)
+        if (plan->precision == NBCS_PREC_MIXED && bps < 0) {
+            for (int c = 0; c < plan->nclasses; ++c) {
+                rc = launch_batch32_class(plan->classes[c], f32, fields, nmax, s);
+                if (rc) return rc;
+            }
+            rc = NBCS_OK;
+        } else if (plan->precision == NBCS_PREC_MIXED) {
             rc = launch_batch32(hdr, f32, fields, plan->nfields, bps, nmax, s);
-        else
+        } else {
             rc = launch_batch64(hdr, reinterpret_cast<const DevFlow64*>(base + lay.off_f64), fields,
                                 plan->nfields, bps, nmax, s);
+        }
         if (rc) return rc;
     }
     if (plan->ftle_blocks > 0) return launch_ftle_batch(fields, plan->nfields, plan->ftle_blocks, s);

@@ -22,19 +22,6 @@
 
 namespace nbcs {
 
-// Threads per block of the single-field integrator, and the width in y of the
-// particle tile a block integrates: at LP = 2 a block takes a 16 x 8 tile of
-// the grid (8 warps, each a 4 x 4 sub-tile).  Measured on the geophysical
-// spline workload (676 x 251 particles): 128-thread 8 x 8 tiles 5.52 ms,
-// 256-thread 16 x 8 tiles 5.24 ms, 8 x 16 tiles 5.36 ms, 32 x 4 tiles 5.43
-// ms; warps of one block share L1 lines of neighbouring trajectories, and the
-// flow is mostly zonal.  The minimum of 3 resident blocks gives the compiler
-// 85 registers a thread; it takes 80 with no spills (24 warps per SM), 5.08
-// ms; a 64-register cap with 4 blocks spilled and took 5.40 ms.
-constexpr int kFm32Block = 256;
-constexpr int kFm32TileJ = 8;
-constexpr int kFm32MinBlocks = 3;
-
 template <class Flow>
 __global__ void __launch_bounds__(kFm32Block, kFm32MinBlocks)
 flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restrict__ x,

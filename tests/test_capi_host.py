@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, n), n
     # the Python binding declares a signature for every entry point
     assert set(names) <= set(_lib.SIGNATURES)
-    assert L.nbcs_abi_version() == 2
+    assert L.nbcs_abi_version() == 3
 
 
 def test_scratch_size_queries():

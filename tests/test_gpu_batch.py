@@ -67,7 +67,7 @@ def test_batch_autotune_and_sizes(nb):
     from numbacs_gb300.batch import FTLEBatch
     fields = _fields(nb)
     b = FTLEBatch(fields, precision="mixed", blocks_per_sm=None, graph=True)
-    assert b.blocks_per_sm >= 1 or b.blocks_per_sm == -1
+    assert b.blocks_per_sm >= 1 or b.blocks_per_sm in (-1, -2)
     b.run()
     torch.cuda.synchronize()
     assert b.particles == sum(f.x.numel() * f.y.numel() for f in fields)
@@ -79,6 +79,18 @@ def test_batch_autotune_and_sizes(nb):
         ti = 16 if f.flow.kind == 2 else 32
         return -(-f.x.numel() // ti) * -(-f.y.numel() // 8)
     assert int(b.plan.tiles) == sum(tiles(f) for f in fields)
+    # flow classes: spline (spherical), double gyre, Bickley; each a contiguous
+    # range of the field table, spline fields at two lanes a particle
+    P = b.plan
+    cl = [P.classes[k] for k in range(P.nclasses)]
+    assert P.nclasses == 3
+    assert sorted(c.kind for c in cl) == [0, 1, 2]
+    assert sum(c.nfields for c in cl) == len(fields)
+    assert sum(int(c.tiles) for c in cl) == int(P.tiles)
+    assert sorted((c.field0, c.field0 + c.nfields) for c in cl)[0][0] == 0
+    for c in cl:
+        assert c.lanes == (2 if c.kind == 2 else 1)
+        assert c.flow >= 0  # one flow per class in this batch: the kernel-argument form
 
 
 def test_batch_extrap_flows_take_the_per_field_schedule(nb):
