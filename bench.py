@@ -631,7 +631,12 @@ def run_batch(wl, rtol, atol, steps):
                          "persistent, %d blocks/SM, warps take chunks" % batch.blocks_per_sm),
             "launch": ("one CUDA graph: a per-field integrator + FTLE launch on each branch"
                        if batch.blocks_per_sm == -2 else
-                       "one integrator launch + one FTLE launch, CUDA graph replay")}
+                       "per flow class one tile-kernel launch (parallel streams) + one FTLE "
+                       "launch, CUDA graph replay" if batch.blocks_per_sm == -1 else
+                       "one integrator launch + one FTLE launch, CUDA graph replay"),
+            "autotune_ms": (batch.tuning or {}).get("ms"),
+            "classes": [{"kind": int(c.kind), "fields": int(c.nfields), "tiles": int(c.tiles)}
+                        for c in batch.plan.classes[:batch.plan.nclasses]]}
 
 
 def train_proposer(rtol, atol, seeds=range(8), t0s=(168.0, 190.0, 215.0), sample=0.22):

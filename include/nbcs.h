@@ -370,7 +370,7 @@ int nbcs_flowmap_log_steps(const nbcs_flow* flow, double t0, double T, const dou
  * plugin whose host program keeps all cudaMalloc calls to itself, or a caller
  * binding this library through a thin FFI with no device allocator of its
  * own.  Same arguments and results as nbcs_ridge_pts, minus the scratch: the
- * scratch is a fixed array compiled into the library (about 8.5 MB, see
+ * scratch is a fixed array compiled into the library (about 8.4 MB, see
  * nbcs_ridge_noalloc_scratch_bytes), which every GPU that loads the library
  * holds until the process exits.  Grids above NBCS_RIDGE_NOALLOC_MAX_POINTS
  * points are rejected with NBCS_ERR_INVALID.  The first call on a device looks

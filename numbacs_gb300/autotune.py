@@ -72,12 +72,14 @@ def tune_batch(batch, candidates=None, force=False):
     if not force:
         hit = _load().get(key)
         if hit is not None:
+            batch.tuning = hit
             return hit["blocks_per_sm"]
     times = {}
     for c in candidates:
         times[c] = _time(lambda: batch.launch(blocks_per_sm=c))
     best = min(times, key=times.get)
-    _store(key, {"blocks_per_sm": best, "ms": times})
+    batch.tuning = {"blocks_per_sm": best, "ms": times}
+    _store(key, batch.tuning)
     return best
 
 

@@ -132,6 +132,7 @@ class FTLEBatch:
         self.max_streams = max(1, int(max_streams))
         self._streams = None
         self._class_streams = None
+        self.tuning = None  # the autotuner's timings of the schedules, when it chose
         # longest work first: particles x |T|
         self._order = sorted(range(len(self.fields)),
                              key=lambda k: -self.fields[k].particles * abs(self.fields[k].T))

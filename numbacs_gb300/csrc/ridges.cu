@@ -8,17 +8,21 @@
 //                    lower*(1-m) + upper*m of the order statistics around it.
 //
 // Percentile: radix selection of the k-th smallest double on order-preserving
-// 64-bit keys, 11 bits per pass (6 passes), then one pass for the smallest key
-// above it (the (k+1)-th order statistic).  Each pass is one launch; the last
+// 64-bit keys, 11 bits per pass (6 passes).  Each pass is one launch; the last
 // block to finish (atomic ticket, no spinning) picks the digit and resets the
-// histogram for the next pass, so no host round trip is needed.
+// histogram for the next pass, so no host round trip is needed.  The last
+// pass also takes the smallest key above the final group (keys that differ
+// from the k-th in a higher digit), so that its last block finds the
+// (k+1)-th order statistic -- the next nonzero bin of its own histogram, or
+// that minimum -- and writes the percentile without another pass.  The
+// selection state starts from a memset of the scratch.
 //
 // Ridge points: pass 1 evaluates the stencil and writes the mask (and, when
 // the caller asks for it, the full point array) and one count per block of
-// points; pass 2 scans the counts; pass 3 ranks the flagged points of each
-// block in row-major order (warp ballots) and writes them compacted, gathering
-// them from the full array when there is one, else re-evaluating the stencil
-// at the flagged points only.
+// points; pass 2 ranks the flagged points of each block in row-major order
+// (warp ballots; each block sums the counts of the blocks before it) and
+// writes them compacted, gathering them from the full array when there is
+// one, else re-evaluating the stencil at the flagged points only.
 // Compiled with -fmad=false: the stencil arithmetic is the reference's.
 #include <math.h>
 
@@ -37,7 +41,7 @@ constexpr int kSelThreads = 512;
 struct SelState {
     unsigned long long prefix;  // key bits chosen so far
     unsigned long long pmask;   // which key bits are chosen
-    unsigned long long next_min;  // smallest key above the k-th key
+    unsigned long long above_inv; // ~(smallest key above the final group); 0: none
     long long rank;             // rank still to find inside the prefix group
     long long eq;               // elements equal to the k-th key (after the last pass)
     unsigned int done;          // ticket of finished blocks in the current pass
@@ -71,35 +75,64 @@ __device__ __forceinline__ double dkey_decode(unsigned long long k)
     return __longlong_as_double((long long)u);
 }
 
-__global__ void sel_init_kernel(SelScratch* s, long long k)
-{
-    for (int b = threadIdx.x; b < kBins; b += blockDim.x) s->hist[b] = 0;
-    if (threadIdx.x == 0) {
-        s->st.prefix = 0;
-        s->st.pmask = 0;
-        s->st.next_min = ~0ull;
-        s->st.rank = k;
-        s->st.eq = 0;
-        s->st.done = 0;
-        s->st.nan_count = s->st.pinf = s->st.ninf = 0;
-        s->st.result = 0.0;
-    }
-}
-
 // one radix pass: histogram the digit at `shift` of the keys in the current
 // prefix group; the last block selects the digit holding rank `rank`.
+// How the last pass turns the k-th and (k+1)-th order statistics into the
+// percentile (numba's rules, ridges.py:48-51).
+struct SelFinish {
+    int mode;  // 0: interpolate; 1: q == 100 (maximum); 2: q == 0 (minimum)
+    double m;  // interpolation weight of the upper statistic
+    double* out;
+};
+
+__device__ void sel_finish(SelScratch* s, long n, unsigned long long kk, unsigned long long up,
+                           const SelFinish& fin)
+{
+    const long long nan_count = (long long)__ldcg(&s->st.nan_count);
+    const long long pinf = (long long)__ldcg(&s->st.pinf), ninf = (long long)__ldcg(&s->st.ninf);
+    double lower = dkey_decode(kk), val;
+    if (nan_count > 0) {
+        val = NAN;
+    } else if (n == 1) {
+        val = lower;
+    } else if (fin.mode == 1) {  // q == 100: maximum
+        val = lower;
+        if ((pinf + ninf) > 0 && !isfinite(val)) val = NAN;
+    } else if (fin.mode == 2) {  // q == 0: minimum, with numba's infinity rules
+        val = lower;
+        if (pinf + ninf > 0) {
+            long long finite = n - (pinf + ninf);
+            if (finite == 0) val = NAN;
+            if (pinf == 1 && n == 2) val = NAN;
+            if (ninf > 1) val = NAN;
+            if (finite == 1 && pinf > 1 && ninf != 1) val = NAN;
+        }
+    } else {
+        double upper = (up == ~0ull) ? lower : dkey_decode(up);
+        val = lower * (1.0 - fin.m) + upper * fin.m;
+    }
+    s->st.result = val;
+    if (fin.out) *fin.out = val;
+}
+
 __global__ void __launch_bounds__(kSelThreads)
-sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, int bits, int first)
+sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, int bits, int first,
+                long long k, SelFinish fin)
 {
     __shared__ unsigned int h[kBins];
     __shared__ unsigned int cnt[3];
+    __shared__ unsigned long long wmax[kSelThreads / 32];
     __shared__ bool is_last;
     for (int b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0;
     if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
     __syncthreads();
-    const unsigned long long prefix = s->st.prefix, pmask = s->st.pmask;
+    // the first pass starts from the zeroed scratch: empty prefix, rank k
+    const unsigned long long prefix = first ? 0ull : s->st.prefix;
+    const unsigned long long pmask = first ? 0ull : s->st.pmask;
+    const bool last_pass = shift == 0;
     const unsigned int dmask = (1u << bits) - 1u;
     unsigned int nn = 0, np = 0, nm = 0;
+    unsigned long long ainv = 0ull;  // ~(smallest key above the group), last pass
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long)gridDim.x * blockDim.x) {
         const unsigned long long u = (unsigned long long)__double_as_longlong(f[i]);
@@ -109,7 +142,10 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
             else if (u == 0xfff0000000000000ull) ++nm;
         }
         const unsigned long long key = dkey(u);
-        if ((key & pmask) != prefix) continue;
+        if ((key & pmask) != prefix) {
+            if (last_pass && (key & pmask) > prefix && ~key > ainv) ainv = ~key;
+            continue;
+        }
         atomicAdd(&h[(unsigned)(key >> shift) & dmask], 1u);
     }
     if (first) {
@@ -117,7 +153,18 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
         if (np) atomicAdd(&cnt[1], np);
         if (nm) atomicAdd(&cnt[2], nm);
     }
+    if (last_pass) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long other = __shfl_xor_sync(0xffffffffu, ainv, o);
+            ainv = other > ainv ? other : ainv;
+        }
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = ainv;
+    }
     __syncthreads();
+    if (last_pass && threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) ainv = wmax[w] > ainv ? wmax[w] : ainv;
+        if (ainv) atomicMax(&s->st.above_inv, ainv);
+    }
     for (int b = threadIdx.x; b <= (int)dmask; b += blockDim.x)
         if (h[b]) atomicAdd(&s->hist[b], h[b]);
     if (first && threadIdx.x == 0) {
@@ -136,7 +183,7 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
     // finds the one thread whose range holds the rank, and that thread walks
     // its own bins (no serial loop over the whole block).
     __shared__ long long wsum[kSelThreads / 32];
-    const long long rank = s->st.rank;
+    const long long rank = first ? k : s->st.rank;
     const int nb = (int)dmask + 1;
     const int per = (nb + blockDim.x - 1) / blockDim.x;
     long long local = 0;
@@ -174,73 +221,35 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
             cum += hb;
         }
         if (b >= nb) b = nb - 1;
+        const unsigned long long kk = prefix | ((unsigned long long)b << shift);
         s->st.rank = rank - cum;
-        s->st.prefix = prefix | ((unsigned long long)b << shift);
+        s->st.prefix = kk;
         s->st.pmask = pmask | ((unsigned long long)dmask << shift);
         s->st.eq = hb;
         s->st.done = 0;
+        if (last_pass) {
+            // the (k+1)-th statistic: the k-th key again while equal keys
+            // remain, else the next nonzero bin of this group, else the
+            // smallest key above the group (or none)
+            unsigned long long up = ~0ull;
+            if (rank - cum + 1 < (long long)hb) {
+                up = kk;
+            } else {
+                for (int c = b + 1; c < nb; ++c)
+                    if (__ldcg(&s->hist[c])) {
+                        up = prefix | (unsigned long long)c;
+                        break;
+                    }
+                if (up == ~0ull) {
+                    const unsigned long long a = __ldcg(&s->st.above_inv);
+                    if (a) up = ~a;
+                }
+            }
+            sel_finish(s, n, kk, up, fin);
+        }
     }
     __syncthreads();
     for (int b = threadIdx.x; b < kBins; b += blockDim.x) s->hist[b] = 0;
-}
-
-// smallest key strictly above the k-th key; the last block writes the result
-__global__ void __launch_bounds__(kSelThreads)
-sel_final_kernel(const double* __restrict__ f, long n, SelScratch* s, int mode, double m,
-                 double* __restrict__ out)
-{
-    __shared__ unsigned long long wmin[kSelThreads / 32];
-    __shared__ bool is_last;
-    const unsigned long long kk = s->st.prefix;
-    unsigned long long mn = ~0ull;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const unsigned long long u = (unsigned long long)__double_as_longlong(f[i]);
-        if (bits_nan(u)) continue;
-        const unsigned long long key = dkey(u);
-        if (key > kk && key < mn) mn = key;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long other = __shfl_xor_sync(0xffffffffu, mn, o);
-        mn = other < mn ? other : mn;
-    }
-    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = mn;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mn = wmin[w] < mn ? wmin[w] : mn;
-        if (mn != ~0ull) atomicMin(&s->st.next_min, mn);
-        __threadfence();
-        is_last = (atomicAdd(&s->st.done, 1u) == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!is_last || threadIdx.x != 0) return;
-    __threadfence();
-    const long long nan_count = (long long)__ldcg(&s->st.nan_count);
-    const long long pinf = (long long)__ldcg(&s->st.pinf), ninf = (long long)__ldcg(&s->st.ninf);
-    double lower = dkey_decode(kk), val;
-    if (nan_count > 0) {
-        val = NAN;
-    } else if (n == 1) {
-        val = lower;
-    } else if (mode == 1) {  // q == 100: maximum
-        val = lower;
-        if ((pinf + ninf) > 0 && !isfinite(val)) val = NAN;
-    } else if (mode == 2) {  // q == 0: minimum, with numba's infinity rules
-        val = lower;
-        if (pinf + ninf > 0) {
-            long long finite = n - (pinf + ninf);
-            if (finite == 0) val = NAN;
-            if (pinf == 1 && n == 2) val = NAN;
-            if (ninf > 1) val = NAN;
-            if (finite == 1 && pinf > 1 && ninf != 1) val = NAN;
-        }
-    } else {
-        unsigned long long up = (s->st.rank + 1 < s->st.eq) ? kk : __ldcg(&s->st.next_min);
-        double upper = (up == ~0ull) ? lower : dkey_decode(up);
-        val = lower * (1.0 - m) + upper * m;
-    }
-    s->st.result = val;
-    if (out) *out = val;
 }
 
 static unsigned sel_grid(long n)
@@ -274,18 +283,17 @@ static int percentile_enqueue(const double* f, long n, double q, double* out, Se
         m = rank - fl;
         k = (long long)(fl - 1.0);
     }
-    sel_init_kernel<<<1, 256, 0, st>>>(s, k);
-    NBCS_LAUNCH_CHECK();
+    // zeroed scratch: empty histogram and counters, no key above the group
+    NBCS_CUDA_TRY(cudaMemsetAsync(s, 0, sizeof(SelScratch), st));
+    const SelFinish fin = {mode, m, out};
     unsigned g = sel_grid(n);
     int shift = 64;
     for (int pass = 0; shift > 0; ++pass) {
         int bits = shift >= kDigitBits ? kDigitBits : shift;
         shift -= bits;
-        sel_pass_kernel<<<g, kSelThreads, 0, st>>>(f, n, s, shift, bits, pass == 0);
+        sel_pass_kernel<<<g, kSelThreads, 0, st>>>(f, n, s, shift, bits, pass == 0, k, fin);
         NBCS_LAUNCH_CHECK();
     }
-    sel_final_kernel<<<g, kSelThreads, 0, st>>>(f, n, s, mode, m, out);
-    NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
 
@@ -395,48 +403,31 @@ ridge_flag_kernel(RidgeIn R, uint8_t* __restrict__ mask, double2* __restrict__ r
     if (threadIdx.x == 0) block_count[blockIdx.x] = tot;
 }
 
-// exclusive scan of the per-block counts (one block); total -> *n_out
-__global__ void __launch_bounds__(1024)
-ridge_scan_kernel(const unsigned int* __restrict__ cnt, long nb, unsigned long long* __restrict__ off,
-                  int64_t* __restrict__ n_out)
-{
-    __shared__ unsigned long long part[1024];
-    const long per = (nb + blockDim.x - 1) / blockDim.x;
-    const long b0 = (long)threadIdx.x * per;
-    unsigned long long s = 0;
-    for (long q = 0; q < per; ++q)
-        if (b0 + q < nb) s += cnt[b0 + q];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        unsigned long long v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    unsigned long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-    for (long q = 0; q < per; ++q) {
-        if (b0 + q < nb) {
-            off[b0 + q] = run;
-            run += cnt[b0 + q];
-        }
-    }
-    if (threadIdx.x == blockDim.x - 1) *n_out = (int64_t)part[blockDim.x - 1];
-}
-
+// The block's first output slot is the sum of the counts of the blocks before
+// it (each block adds up at most a few thousand counts: no separate scan
+// launch); the last block also writes the total.
 __global__ void __launch_bounds__(kRidgeThreads)
 ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
-                     const unsigned long long* __restrict__ off, const double2* __restrict__ full,
-                     double2* __restrict__ out)
+                     const unsigned int* __restrict__ block_count, const double2* __restrict__ full,
+                     double2* __restrict__ out, int64_t* __restrict__ n_out)
 {
     __shared__ unsigned int wsum[kRidgeThreads / 32];
+    __shared__ unsigned long long wpre[kRidgeThreads / 32];
     const long n = (long)R.nx * R.ny;
     double dx, dy;
     ridge_spacing(R, &dx, &dy);
     const double fmin = R.fmin_ptr ? *R.fmin_ptr : R.fmin_val;
     const long base = (long)blockIdx.x * R.rounds * kRidgeThreads;
-    unsigned long long run = off[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long pre = 0;
+    for (unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += block_count[b];
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
+    if (lane == 0) wpre[warp] = pre;
+    __syncthreads();
+    unsigned long long run = 0;
+    for (int w = 0; w < kRidgeThreads / 32; ++w) run += wpre[w];
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+        *n_out = (int64_t)(run + block_count[blockIdx.x]);
 #pragma unroll 1
     for (int r = 0; r < R.rounds; ++r) {
         long k = base + (long)r * kRidgeThreads + threadIdx.x;
@@ -502,7 +493,7 @@ extern "C" size_t nbcs_ridge_scratch_bytes(int32_t nx, int32_t ny)
     if (nx < 0 || ny < 0) return 0;
     long nb = ridge_blocks(nx, ny);
     return align256(sizeof(SelScratch)) + align256(sizeof(unsigned int) * (size_t)nb) +
-           align256(sizeof(unsigned long long) * (size_t)nb) + align256((size_t)nx * ny);
+           align256((size_t)nx * ny);
 }
 
 // Ridge flags, points and compaction with the threshold f_min either taken
@@ -531,8 +522,6 @@ static int ridge_run(const double* f, const double* evec_max, const double* x, i
     p += align256(sizeof(SelScratch));
     unsigned int* cnt = reinterpret_cast<unsigned int*>(p);
     p += align256(sizeof(unsigned int) * (size_t)nb);
-    unsigned long long* off = reinterpret_cast<unsigned long long*>(p);
-    p += align256(sizeof(unsigned long long) * (size_t)nb);
     uint8_t* mask = mask_out ? mask_out : reinterpret_cast<uint8_t*>(p);
 
     RidgeIn R;
@@ -556,10 +545,9 @@ static int ridge_run(const double* f, const double* evec_max, const double* x, i
     ridge_flag_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
         R, mask, reinterpret_cast<double2*>(rpts_full), cnt);
     NBCS_LAUNCH_CHECK();
-    ridge_scan_kernel<<<1, 1024, 0, st>>>(cnt, nb, off, n_out);
-    NBCS_LAUNCH_CHECK();
     ridge_compact_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
-        R, mask, off, reinterpret_cast<const double2*>(rpts_full), reinterpret_cast<double2*>(pts_out));
+        R, mask, cnt, reinterpret_cast<const double2*>(rpts_full), reinterpret_cast<double2*>(pts_out),
+        n_out);
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
@@ -595,7 +583,7 @@ extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, cons
 // a caller that binds this library through a thin FFI and has no device
 // allocator of its own.  nbcs_ridge_pts_noalloc gives them ridge extraction
 // without a scratch argument: its scratch is the file-scope array below,
-// sized for grids of up to NBCS_RIDGE_NOALLOC_MAX_POINTS points (about 8.5 MB,
+// sized for grids of up to NBCS_RIDGE_NOALLOC_MAX_POINTS points (about 8.4 MB,
 // held by every GPU that loads the library until the process exits).
 //
 // The array's name is only a host-side stand-in, so the device address is
@@ -605,8 +593,8 @@ extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, cons
 // context; it is not refreshed after cudaDeviceReset.
 // Every call shares the array and leaves its contents behind; the kernels
 // re-initialise everything they read (the selection state and histogram, the
-// per-block counts, offsets and mask), and calls whose work overlaps on the
-// GPU race on it.
+// per-block counts and mask), and calls whose work overlaps on the GPU race on
+// it.
 
 namespace nbcs {
 
@@ -619,7 +607,6 @@ constexpr long kNoallocBlocks =
         : kRidgeFillBlocks + 1;
 constexpr size_t kNoallocScratchBytes =
     align256c(sizeof(SelScratch)) + align256c(sizeof(unsigned int) * kNoallocBlocks) +
-    align256c(sizeof(unsigned long long) * kNoallocBlocks) +
     align256c((size_t)NBCS_RIDGE_NOALLOC_MAX_POINTS);
 
 static __device__ __align__(256) unsigned char g_ridge_noalloc_scratch[kNoallocScratchBytes];
