@@ -260,10 +260,11 @@ int nbcs_ftle_from_eig(const double* eigval, int64_t n, int64_t stride, double T
 /* Fused C_eig_2D + ftle_from_eig(eigvals[...,1]) + eigvecs[...,:,1]:
  * flowmap -> ftle (nx,ny) and evec_max (nx,ny,2) in one pass (the inputs of
  * ftle_ridge_pts).  The scaling divisions (1/(2dx), 1/(2dy), 1/(2|T|)) are
- * products with reciprocals and the eigenvector is normalised by a reciprocal
- * square root, so the values are within a few ulp of nbcs_c_eig_2d +
- * nbcs_ftle_from_eig rather than bit-identical (those two keep the
- * reference's IEEE divisions). */
+ * products with reciprocals, the eigenvector is normalised by a reciprocal
+ * square root and the log's mantissa part is an FP32 log1p, so the
+ * eigenvector is within a few ulp and the FTLE within ~3e-7 relative of
+ * nbcs_c_eig_2d + nbcs_ftle_from_eig rather than bit-identical (those two
+ * keep the reference's IEEE arithmetic). */
 int nbcs_ftle_evec_2d(const double* flowmap, int32_t nx, int32_t ny, double T, double dx,
                       double dy, const uint8_t* mask, double* ftle, double* evec_max,
                       void* stream);
@@ -390,6 +391,21 @@ int nbcs_ridge_pts_noalloc(const double* f, const double* evec_max, const double
 
 /* ------------------------------------------------------------ measurement */
 /* No counterpart in the reference (which has no GPU path). */
+
+/* Bounds-checked build (libnbcs_check.so, built with -DNBCS_CHECK by
+ * `python -m numbacs_gb300.build --check`): the accesses whose index comes
+ * from data -- the spline coefficient gathers of both integrators (the cell
+ * of a particle's position), the composition's bilinear gathers, the
+ * labelling's parent links -- test it against their buffer, skip the access
+ * and set a bit instead of faulting.  nbcs_check_enabled() is 1 in that
+ * build, 0 in the normal one (where nbcs_check_bits always reports 0).
+ * nbcs_check_bits ORs the bits set since the last reset into *bits
+ * (synchronous; reset != 0 clears them).  No counterpart in the reference. */
+#define NBCS_CHECK_SPLINE_GATHER 0x1u
+#define NBCS_CHECK_COMPOSE_GATHER 0x2u
+#define NBCS_CHECK_LABEL_LINK 0x4u
+int nbcs_check_enabled(void);
+int nbcs_check_bits(uint32_t* bits, int32_t reset);
 
 /* Number of kernels this library has launched in the process so far. */
 unsigned long long nbcs_launch_count(void);

@@ -8,7 +8,9 @@ import ctypes
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_build", "libnbcs.so")
+# NBCS_LIB selects another build of the library (the bounds-checked
+# _build_check/libnbcs_check.so, for instance)
+LIB_PATH = os.environ.get("NBCS_LIB") or os.path.join(_HERE, "_build", "libnbcs.so")
 
 NBCS_OK = 0
 PARTICLE_OK, PARTICLE_MASKED = 0, 1
@@ -121,6 +123,8 @@ SIGNATURES = {
     "nbcs_ridge_pts_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp,
                                               _vp, _vp, _vp]),
     "nbcs_launch_count": (ctypes.c_ulonglong, []),
+    "nbcs_check_enabled": (ctypes.c_int, []),
+    "nbcs_check_bits": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32), _i32]),
     "nbcs_probe_fma": (ctypes.c_int, [_i32, _i64, _vp, ctypes.POINTER(ctypes.c_double), _vp]),
 }
 

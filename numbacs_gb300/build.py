@@ -7,6 +7,8 @@ precision integrator is compiled with FMA contraction on.
 
     python -m numbacs_gb300.build          # build if sources changed
     python -m numbacs_gb300.build --force  # rebuild everything
+    python -m numbacs_gb300.build --check  # the bounds-checked debug library,
+                                           # _build_check/libnbcs_check.so (-DNBCS_CHECK)
 """
 import concurrent.futures as cf
 import os
@@ -19,6 +21,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnbcs.so")
+BUILD_CHECK = os.path.join(HERE, "_build_check")
+LIB_CHECK = os.path.join(BUILD_CHECK, "libnbcs_check.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -64,8 +68,8 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, extra, verbose):
-    obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+def _compile(src, extra, verbose, bdir=BUILD):
+    obj = os.path.join(bdir, src.replace(".cu", ".o"))
     cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + ARCH + COMMON + extra
     if verbose:
         cmd += ["-Xptxas", "-v"]
@@ -75,34 +79,40 @@ def _compile(src, extra, verbose):
     return obj, r.stderr
 
 
-def build(force=False, verbose=False, jobs=None):
-    """Compile every CUDA source for sm_103a and link libnbcs.so. Returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, jobs=None, check=False):
+    """Compile every CUDA source for sm_103a and link libnbcs.so (with
+    check=True: the bounds-checked libnbcs_check.so, -DNBCS_CHECK, in its own
+    build folder). Returns its path."""
+    bdir, lib = (BUILD_CHECK, LIB_CHECK) if check else (BUILD, LIB)
+    flag = ["-DNBCS_CHECK"] if check else []
+    os.makedirs(bdir, exist_ok=True)
     hdrs = _deps()
     todo = []
     for src, extra in SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(bdir, src.replace(".cu", ".o"))
         if force or _stale(obj, [os.path.join(CSRC, src)] + hdrs):
-            todo.append((src, extra))
+            todo.append((src, extra + flag))
     logs = []
     if todo:
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(todo), os.cpu_count() or 4)) as ex:
-            for obj, log in ex.map(lambda a: _compile(a[0], a[1], verbose), todo):
+            for obj, log in ex.map(lambda a: _compile(a[0], a[1], verbose, bdir), todo):
                 logs.append((obj, log))
-    objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s, _ in SOURCES]
-    if force or todo or _stale(LIB, objs):
-        tmp = LIB + ".tmp%d" % os.getpid()
+    objs = [os.path.join(bdir, s.replace(".cu", ".o")) for s, _ in SOURCES]
+    LIB_ = lib
+    if force or todo or _stale(LIB_, objs):
+        tmp = LIB_ + ".tmp%d" % os.getpid()
         cmd = [nvcc(), "-shared", "-cudart", "shared", "-o", tmp] + objs + ARCH
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-        os.replace(tmp, LIB)
+        os.replace(tmp, LIB_)
     if verbose:
         for obj, log in logs:
             sys.stderr.write("== %s\n%s" % (os.path.basename(obj), log))
-    return LIB
+    return LIB_
 
 
 if __name__ == "__main__":
-    path = build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    path = build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                 check="--check" in sys.argv)
     print(path)

@@ -80,6 +80,49 @@ int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int p
 
 }  // namespace nbcs
 
+namespace nbcs {
+
+#ifdef NBCS_CHECK
+static int (*g_check_readers[32])(unsigned int*, int);
+static int g_check_nreaders = 0;
+
+int register_check_reader(int (*read)(unsigned int*, int))
+{
+    // static initialisers of the library's units, run once at load
+    if (g_check_nreaders < 32) g_check_readers[g_check_nreaders++] = read;
+    return g_check_nreaders;
+}
+#endif
+
+}  // namespace nbcs
+
+extern "C" int nbcs_check_enabled(void)
+{
+#ifdef NBCS_CHECK
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+extern "C" int nbcs_check_bits(uint32_t* bits, int32_t reset)
+{
+    if (!bits) return nbcs::set_error(NBCS_ERR_INVALID, "check_bits: NULL");
+    *bits = 0;
+#ifdef NBCS_CHECK
+    for (int k = 0; k < nbcs::g_check_nreaders; ++k) {
+        unsigned int b = 0;
+        int e = nbcs::g_check_readers[k](&b, reset);
+        if (e) return nbcs::set_error(NBCS_ERR_CUDA, "check_bits: %s",
+                                      cudaGetErrorString((cudaError_t)e));
+        *bits |= b;
+    }
+#else
+    (void)reset;
+#endif
+    return NBCS_OK;
+}
+
 extern "C" int nbcs_abi_version(void) { return NBCS_ABI_VERSION; }
 
 extern "C" const char* nbcs_last_error(void) { return nbcs::g_err; }

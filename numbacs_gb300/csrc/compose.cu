@@ -44,6 +44,9 @@ __device__ __forceinline__ double2 bilinear2(const double2* __restrict__ f, cons
     double l0, l1;
     const int i = lin_locate(g.x0, g.dinvx, g.nx, px, &l0);
     const int j = lin_locate(g.y0, g.dinvy, g.ny, py, &l1);
+    if (!NBCS_CHECKED(i >= 0 && i <= g.nx - 2 && j >= 0 && j <= g.ny - 2,
+                      NBCS_CHECK_COMPOSE_GATHER))
+        return make_double2(0.0, 0.0);
     const double2* r0 = f + (long)i * g.ny + j;
     const double2* r1 = r0 + g.ny;
     const double2 f00 = __ldg(r0), f01 = __ldg(r0 + 1), f10 = __ldg(r1), f11 = __ldg(r1 + 1);

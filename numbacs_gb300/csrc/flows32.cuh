@@ -242,6 +242,19 @@ __device__ __forceinline__ void ldg_row8(const float* __restrict__ p, float* r)
         : "l"(p));
 }
 
+// Stencil row at quad entry e: one 256-bit load (in the checked build only
+// when e lies inside the (nt+2)(nx+2)(ny+2)-entry block; zeros otherwise).
+__device__ __forceinline__ void spline_row32(const SplineGridF& g, const float* __restrict__ c,
+                                             unsigned e, float* p)
+{
+    if (NBCS_CHECKED(e < (unsigned)g.st * (unsigned)(g.ax[0].n + 2), NBCS_CHECK_SPLINE_GATHER)) {
+        ldg_row8(c + 8 * (size_t)e, p);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) p[k] = 0.0f;
+    }
+}
+
 template <int LP>
 __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float* __restrict__ c,
                                                  int it, int ix, int iy, float ft, const float* wx,
@@ -264,7 +277,7 @@ __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const flo
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             float p[8];
-            ldg_row8(c + 8 * (size_t)(e0 + (unsigned)b * (unsigned)g.sx), p);
+            spline_row32(g, c, e0 + (unsigned)b * (unsigned)g.sx, p);
             const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
             const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
             su = fmaf(wx[b], bu, su);
@@ -322,7 +335,7 @@ __device__ __forceinline__ void spline_eval_uv32_grad(const SplineGridF& g,
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             float p[8];
-            ldg_row8(c + 8 * (size_t)(e0 + (unsigned)b * (unsigned)g.sx), p);
+            spline_row32(g, c, e0 + (unsigned)b * (unsigned)g.sx, p);
             const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
             const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
             const float du = fmaf(dwy[0], p[0], fmaf(dwy[1], p[2], fmaf(dwy[2], p[4], dwy[3] * p[6])));
@@ -379,7 +392,7 @@ __device__ __forceinline__ void spline_eval_uv32_lin(const SplineGridF& g, const
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             float p[8];
-            ldg_row8(c + 8 * (size_t)(e0 + (unsigned)b * (unsigned)g.sx), p);
+            spline_row32(g, c, e0 + (unsigned)b * (unsigned)g.sx, p);
             const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
             const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
             const float du = fmaf(dwy[0], p[0], fmaf(dwy[1], p[2], fmaf(dwy[2], p[4], dwy[3] * p[6])));

@@ -115,8 +115,16 @@ __device__ __forceinline__ void spline_sum_uv64(const SplineGrid& g, const doubl
         double su = 0.0, sv = 0.0;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const double2* row = c + (size_t)(it + a) * g.st + (size_t)(ix + b) * g.sx + iy;
-            double2 r0 = __ldg(row), r1 = __ldg(row + 1), r2 = __ldg(row + 2), r3 = __ldg(row + 3);
+            const size_t e = (size_t)(it + a) * g.st + (size_t)(ix + b) * g.sx + iy;
+            const double2* row = c + e;
+            double2 r0 = make_double2(0.0, 0.0), r1 = r0, r2 = r0, r3 = r0;
+            if (NBCS_CHECKED(e + 3 < (size_t)g.st * (size_t)(g.n[0] + 2),
+                             NBCS_CHECK_SPLINE_GATHER)) {
+                r0 = __ldg(row);
+                r1 = __ldg(row + 1);
+                r2 = __ldg(row + 2);
+                r3 = __ldg(row + 3);
+            }
             double bu = w2[0] * r0.x + w2[1] * r1.x + w2[2] * r2.x + w2[3] * r3.x;
             double bv = w2[0] * r0.y + w2[1] * r1.y + w2[2] * r2.y + w2[3] * r3.y;
             su += w1[b] * bu;

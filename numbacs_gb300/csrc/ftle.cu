@@ -22,6 +22,7 @@ struct Grad {
 __device__ __forceinline__ Grad grad_stencil(const double2* __restrict__ F, long k, int ny,
                                              double dx, double dy)
 {
+    // interior points only: k - ny >= 0 and k + ny < nx * ny by the caller's test
     double2 ip = __ldg(F + k + ny), im = __ldg(F + k - ny);
     double2 jp = __ldg(F + k + 1), jm = __ldg(F + k - 1);
     Grad g;
@@ -176,9 +177,11 @@ __global__ void ceig_aux_kernel(const double2* __restrict__ F, int nx, int ny, i
 // 1 / (2 dy) and the FTLE's 1 / (2 |T|) -- taken as products with reciprocals
 // computed once on the host, and the eigenvector normalised by a reciprocal
 // square root.  The smaller eigenvalue, which this entry point does not
-// return, is not formed.  Within a few ulp of the C_eig_2D / ftle_from_eig
-// values (FTLE relative error ~1e-15 where lambda_max > 1 + 1e-6); the FP64
-// divisions of the bit-exact kernels were 60 % of this stencil's FP64 work.
+// return, is not formed, and the log of the FTLE takes its mantissa part on
+// the FP32 pipe (below).  The eigenvector is within a few ulp of C_eig_2D's
+// and the FTLE within ~3e-7 relative of ftle_from_eig's where
+// lambda_max > 1 + 1e-6; the FP64 divisions and log of the bit-exact kernels
+// were most of this stencil's FP64 work.
 __device__ __forceinline__ void ftle_evec_point(const double2* __restrict__ F, long k, int ny,
                                                 double rdx, double rdy, double rden, double* f,
                                                 double2* v)
@@ -209,7 +212,23 @@ __device__ __forceinline__ void ftle_evec_point(const double2* __restrict__ F, l
         ex = -ex;
         ey = -ey;
     }
-    *f = l1 > 1.0 ? log(l1) * rden : 0.0;
+    // FTLE = log(lambda) / (2|T|) to ~3e-7 relative (the contract is 1e-5):
+    // lambda = 2^e m with m in [1, 2), log(lambda) = e ln 2 + log1p(m - 1); the
+    // exponent term in FP64 and m - 1 exact, its log1p on the FP32 pipe (the
+    // FP64 log was the largest FP64 cost left once the divisions were gone)
+    double fv = 0.0;
+    if (l1 > 1.0) {
+        const long long bits = __double_as_longlong(l1);
+        const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+        if (e == 1024) {
+            fv = l1 * rden;  // +inf
+        } else {
+            const double m =
+                __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+            fv = ((double)e * 0.6931471805599453 + (double)log1pf((float)(m - 1.0))) * rden;
+        }
+    }
+    *f = fv;
     *v = make_double2(ex, ey);
 }
 

@@ -25,6 +25,8 @@ __device__ __forceinline__ int ccl_find(int* parent, int x)
     for (;;) {
         int p = parent[x];
         if (p == x) return x;
+        // a link always points down to a smaller index of the same component
+        if (!NBCS_CHECKED(p >= 0 && p < x, NBCS_CHECK_LABEL_LINK)) return x;
         int gp = parent[p];
         if (gp != p) parent[x] = gp;  // path halving: gp is an ancestor of x
         x = p;
@@ -77,7 +79,10 @@ __global__ void ccl_merge_kernel(int nx, int ny, int* parent, int* err)
 // thread's final `parent[x] = root` could put a non-root ancestor back.
 __device__ __forceinline__ int ccl_root(const int* parent, int x)
 {
-    for (int p = parent[x]; p != x; p = parent[x]) x = p;
+    for (int p = parent[x]; p != x; p = parent[x]) {
+        if (!NBCS_CHECKED(p >= 0 && p < x, NBCS_CHECK_LABEL_LINK)) return x;
+        x = p;
+    }
     return x;
 }
 
@@ -148,7 +153,7 @@ __global__ void ccl_propagate_kernel(long n, const int* __restrict__ parent, int
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
         const int p = parent[k];
         if (p < 0) labels[k] = 0;
-        else if (p != (int)k) labels[k] = labels[p];
+        else if (p != (int)k && NBCS_CHECKED(p < k, NBCS_CHECK_LABEL_LINK)) labels[k] = labels[p];
     }
 }
 

@@ -39,6 +39,39 @@ struct NvtxRange {
 };
 #define NBCS_RANGE() ::nbcs::NvtxRange nbcs_range_(__func__)
 
+// Bounds-checked build (compiled with -DNBCS_CHECK; `python -m
+// numbacs_gb300.build --check` builds it beside the normal library).  Every
+// checked access (the data-dependent ones: spline gathers, composition
+// gathers, labelling links) tests its index against the extent of its buffer;
+// a failed test sets its bit (NBCS_CHECK_* in nbcs.h) in this translation
+// unit's word and the access is skipped, so a bad index is reported by
+// nbcs_check_bits instead of faulting the GPU.  In the normal build the test
+// compiles to nothing.
+#ifdef NBCS_CHECK
+static __device__ unsigned int g_nbcs_check_word;
+#define NBCS_CHECKED(cond, bit) \
+    ((cond) ? true : (atomicOr(&g_nbcs_check_word, (unsigned)(bit)), false))
+// each unit registers a reader of its own word with the library (capi.cu)
+int register_check_reader(int (*read)(unsigned int* bits, int reset));
+namespace {
+int read_check_word(unsigned int* bits, int reset)
+{
+    unsigned int w = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&w, g_nbcs_check_word, sizeof(w));
+    if (e != cudaSuccess) return (int)e;
+    *bits |= w;
+    if (reset) {
+        const unsigned int zero = 0;
+        e = cudaMemcpyToSymbol(g_nbcs_check_word, &zero, sizeof(zero));
+    }
+    return (int)e;
+}
+const int g_check_reader_registered = register_check_reader(&read_check_word);
+}  // namespace
+#else
+#define NBCS_CHECKED(cond, bit) true
+#endif
+
 // Number of SMs of the current device (cached per device).
 int sm_count();
 

@@ -19,8 +19,9 @@
 //
 // Ridge points: pass 1 evaluates the stencil and writes the mask (and, when
 // the caller asks for it, the full point array) and one count per block of
-// points; pass 2 ranks the flagged points of each block in row-major order
-// (warp ballots; each block sums the counts of the blocks before it) and
+// points (and per group of 64 blocks); pass 2 ranks the flagged points of each
+// block in row-major order (warp ballots; each block adds up the counts before
+// it from the group sums and its own group's block counts) and
 // writes them compacted, gathering them from the full array when there is
 // one, else re-evaluating the stencil at the flagged points only.
 // Compiled with -fmad=false: the stencil arithmetic is the reference's.
@@ -123,6 +124,8 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
     __shared__ unsigned int cnt[3];
     __shared__ unsigned long long wmax[kSelThreads / 32];
     __shared__ bool is_last;
+    __shared__ int sel_b, sel_same, next_bin;
+    __shared__ unsigned long long sel_kk;
     for (int b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0;
     if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
     __syncthreads();
@@ -227,28 +230,39 @@ sel_pass_kernel(const double* __restrict__ f, long n, SelScratch* s, int shift, 
         s->st.pmask = pmask | ((unsigned long long)dmask << shift);
         s->st.eq = hb;
         s->st.done = 0;
-        if (last_pass) {
-            // the (k+1)-th statistic: the k-th key again while equal keys
-            // remain, else the next nonzero bin of this group, else the
-            // smallest key above the group (or none)
-            unsigned long long up = ~0ull;
-            if (rank - cum + 1 < (long long)hb) {
-                up = kk;
-            } else {
-                for (int c = b + 1; c < nb; ++c)
-                    if (__ldcg(&s->hist[c])) {
-                        up = prefix | (unsigned long long)c;
-                        break;
-                    }
-                if (up == ~0ull) {
-                    const unsigned long long a = __ldcg(&s->st.above_inv);
-                    if (a) up = ~a;
-                }
-            }
-            sel_finish(s, n, kk, up, fin);
-        }
+        sel_b = b;
+        sel_kk = kk;
+        sel_same = (rank - cum + 1 < (long long)hb) ? 1 : 0;
     }
     __syncthreads();
+    if (last_pass) {
+        // the (k+1)-th statistic: the k-th key again while equal keys remain,
+        // else the next nonzero bin of this group (a block-wide min over the
+        // bins above the selected one), else the smallest key above the group
+        if (threadIdx.x == 0) next_bin = nb;
+        __syncthreads();
+        if (!sel_same) {
+            for (int c = sel_b + 1 + (int)threadIdx.x; c < nb; c += blockDim.x)
+                if (__ldcg(&s->hist[c])) {
+                    atomicMin(&next_bin, c);
+                    break;
+                }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long up = ~0ull;
+            if (sel_same) {
+                up = sel_kk;
+            } else if (next_bin < nb) {
+                up = prefix | (unsigned long long)next_bin;
+            } else {
+                const unsigned long long a = __ldcg(&s->st.above_inv);
+                if (a) up = ~a;
+            }
+            sel_finish(s, n, sel_kk, up, fin);
+        }
+        __syncthreads();
+    }
     for (int b = threadIdx.x; b < kBins; b += blockDim.x) s->hist[b] = 0;
 }
 
@@ -375,9 +389,13 @@ __device__ __forceinline__ bool ridge_at(const RidgeIn& R, double fmin, double d
     return false;
 }
 
+// Blocks per group of the two-level count prefix: a compaction block adds
+// the group sums before its own group and the counts before it in its group.
+constexpr int kRidgeGroup = 64;
+
 __global__ void __launch_bounds__(kRidgeThreads)
 ridge_flag_kernel(RidgeIn R, uint8_t* __restrict__ mask, double2* __restrict__ rpts,
-                  unsigned int* __restrict__ block_count)
+                  unsigned int* __restrict__ block_count, unsigned int* __restrict__ group_count)
 {
     const long n = (long)R.nx * R.ny;
     double dx, dy;
@@ -400,15 +418,20 @@ ridge_flag_kernel(RidgeIn R, uint8_t* __restrict__ mask, double2* __restrict__ r
     __syncthreads();
     if (c) atomicAdd(&tot, c);
     __syncthreads();
-    if (threadIdx.x == 0) block_count[blockIdx.x] = tot;
+    if (threadIdx.x == 0) {
+        block_count[blockIdx.x] = tot;
+        if (tot) atomicAdd(&group_count[blockIdx.x / kRidgeGroup], tot);
+    }
 }
 
 // The block's first output slot is the sum of the counts of the blocks before
-// it (each block adds up at most a few thousand counts: no separate scan
-// launch); the last block also writes the total.
+// it: the group sums of the groups before its own plus the counts before it in
+// its group (a few hundred loads at most on a 4001 x 4001 field: no separate
+// scan launch); the last block also writes the total.
 __global__ void __launch_bounds__(kRidgeThreads)
 ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
-                     const unsigned int* __restrict__ block_count, const double2* __restrict__ full,
+                     const unsigned int* __restrict__ block_count,
+                     const unsigned int* __restrict__ group_count, const double2* __restrict__ full,
                      double2* __restrict__ out, int64_t* __restrict__ n_out)
 {
     __shared__ unsigned int wsum[kRidgeThreads / 32];
@@ -420,7 +443,10 @@ ridge_compact_kernel(RidgeIn R, const uint8_t* __restrict__ mask,
     const long base = (long)blockIdx.x * R.rounds * kRidgeThreads;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long pre = 0;
-    for (unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += block_count[b];
+    const unsigned g0 = blockIdx.x / kRidgeGroup;
+    for (unsigned q = threadIdx.x; q < g0; q += blockDim.x) pre += group_count[q];
+    for (unsigned b = g0 * kRidgeGroup + threadIdx.x; b < blockIdx.x; b += blockDim.x)
+        pre += block_count[b];
     for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
     if (lane == 0) wpre[warp] = pre;
     __syncthreads();
@@ -492,8 +518,9 @@ extern "C" size_t nbcs_ridge_scratch_bytes(int32_t nx, int32_t ny)
 {
     if (nx < 0 || ny < 0) return 0;
     long nb = ridge_blocks(nx, ny);
+    const long ng = (nb + kRidgeGroup - 1) / kRidgeGroup;
     return align256(sizeof(SelScratch)) + align256(sizeof(unsigned int) * (size_t)nb) +
-           align256((size_t)nx * ny);
+           align256(sizeof(unsigned int) * (size_t)ng) + align256((size_t)nx * ny);
 }
 
 // Ridge flags, points and compaction with the threshold f_min either taken
@@ -522,6 +549,9 @@ static int ridge_run(const double* f, const double* evec_max, const double* x, i
     p += align256(sizeof(SelScratch));
     unsigned int* cnt = reinterpret_cast<unsigned int*>(p);
     p += align256(sizeof(unsigned int) * (size_t)nb);
+    const long ng = (nb + kRidgeGroup - 1) / kRidgeGroup;
+    unsigned int* gcnt = reinterpret_cast<unsigned int*>(p);
+    p += align256(sizeof(unsigned int) * (size_t)ng);
     uint8_t* mask = mask_out ? mask_out : reinterpret_cast<uint8_t*>(p);
 
     RidgeIn R;
@@ -542,12 +572,13 @@ static int ridge_run(const double* f, const double* evec_max, const double* x, i
         if (rc) return rc;
         R.fmin_ptr = &sel->st.result;
     }
+    NBCS_CUDA_TRY(cudaMemsetAsync(gcnt, 0, sizeof(unsigned int) * (size_t)ng, st));
     ridge_flag_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
-        R, mask, reinterpret_cast<double2*>(rpts_full), cnt);
+        R, mask, reinterpret_cast<double2*>(rpts_full), cnt, gcnt);
     NBCS_LAUNCH_CHECK();
     ridge_compact_kernel<<<(unsigned)nb, kRidgeThreads, 0, st>>>(
-        R, mask, cnt, reinterpret_cast<const double2*>(rpts_full), reinterpret_cast<double2*>(pts_out),
-        n_out);
+        R, mask, cnt, gcnt, reinterpret_cast<const double2*>(rpts_full),
+        reinterpret_cast<double2*>(pts_out), n_out);
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }
@@ -593,8 +624,8 @@ extern "C" int nbcs_ridge_pts_fmin(const double* f, const double* evec_max, cons
 // context; it is not refreshed after cudaDeviceReset.
 // Every call shares the array and leaves its contents behind; the kernels
 // re-initialise everything they read (the selection state and histogram, the
-// per-block counts and mask), and calls whose work overlaps on the GPU race on
-// it.
+// per-block and per-group counts and the mask), and calls whose work overlaps
+// on the GPU race on it.
 
 namespace nbcs {
 
@@ -607,6 +638,7 @@ constexpr long kNoallocBlocks =
         : kRidgeFillBlocks + 1;
 constexpr size_t kNoallocScratchBytes =
     align256c(sizeof(SelScratch)) + align256c(sizeof(unsigned int) * kNoallocBlocks) +
+    align256c(sizeof(unsigned int) * ((kNoallocBlocks + kRidgeGroup - 1) / kRidgeGroup)) +
     align256c((size_t)NBCS_RIDGE_NOALLOC_MAX_POINTS);
 
 static __device__ __align__(256) unsigned char g_ridge_noalloc_scratch[kNoallocScratchBytes];

@@ -54,10 +54,10 @@ def test_ftle_and_eig_parity(nb, orc, shape):
         # reciprocal square root: within a few ulp of C_eig_2D + ftle_from_eig
         fe, ve = nb.ftle_evec_2D(fm, -10.0, dx, dy, mask=m)
         ofe = orc.ftle_from_eig(oev[..., 1], -10.0)
-        # (the contract is 1e-5 relative where lambda_max > 1 + 1e-6; next to
-        # lambda = 1 the log cancels, and a few ulp of lambda are ~1e-10 of it)
+        # (the contract is 1e-5 relative where lambda_max > 1 + 1e-6; the
+        # fused stencil's log takes its mantissa part in FP32: ~3e-7)
         nondeg = oev[..., 1] > 1.0 + 1e-6
-        np.testing.assert_allclose(fe[nondeg], ofe[nondeg], rtol=1e-8, atol=0)
+        np.testing.assert_allclose(fe[nondeg], ofe[nondeg], rtol=1e-6, atol=0)
         assert np.abs(fe[~nondeg] - ofe[~nondeg]).max(initial=0.0) <= 1e-7
         assert np.all(fe[oev[..., 1] <= 1.0 - 1e-9] == 0.0)
         sep = oev[..., 1] - oev[..., 0] > 1e-6 * np.abs(oev[..., 1])
