@@ -77,7 +77,13 @@ def tune_batch(batch, candidates=None, force=False):
     times = {}
     for c in candidates:
         times[c] = _time(lambda: batch.launch(blocks_per_sm=c))
-    best = min(times, key=times.get)
+    # within 2 % of the fastest, prefer the schedule with the fewest launches:
+    # a persistent grid (one integrator launch), then per-class tile kernels
+    # (one per flow class), then per-field launches
+    fastest = min(times.values())
+    launches = lambda c: 0 if c >= 0 else (1 if c == -1 else 2)  # noqa: E731
+    best = min((c for c in times if times[c] <= 1.02 * fastest),
+               key=lambda c: (launches(c), times[c]))
     batch.tuning = {"blocks_per_sm": best, "ms": times}
     _store(key, batch.tuning)
     return best
