@@ -16,7 +16,8 @@ the same way and reported beside it).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Under torchrun each rank integrates its own field (t0 + rank hours): weak
-scaling, no collective on the data path.
+scaling, no collective on the data path; the accuracy ladder and the other
+single-GPU legs run only when N = 1.
 """
 import argparse
 import json
@@ -316,7 +317,12 @@ def run_ours(args, rank, world):
     else:
         rtol, atol = HEADLINE_RTOL, HEADLINE_ATOL
     accuracy, truth, rules = None, None, None
-    if not args.quick and not args.rtol:
+    # under torchrun (N > 1) every rank times the headline step and its e2e
+    # leg; the accuracy ladder and the auxiliary legs (single-GPU quantities)
+    # run only on one GPU, so that a scaling run holds its GPUs for little
+    # more than the timed steps
+    solo = world == 1
+    if not args.quick and not args.rtol and solo:
         truth = nb.flowmap_grid_2D(flow, t0, T, x, y, prm, rtol=1e-12, atol=1e-14,
                                    return_status=True)[0]
         ladder, rules = accuracy_ladder(nb, wl, x, y, truth)
@@ -346,7 +352,7 @@ def run_ours(args, rank, world):
     # the plain controller on the headline workload, used for the headline
     # step only when it is faster and meets the same accuracy rule
     proposer, learned, pmode = None, None, 1
-    if prec == "mixed" and not args.quick and not args.no_learned:
+    if prec == "mixed" and not args.quick and not args.no_learned and solo:
         sp, learned = train_proposer(rtol, atol)
         box = ((wl["lon"][0], wl["lon"][-1]), (wl["lat"][0], wl["lat"][-1]))
         modes = {}
@@ -556,10 +562,10 @@ def run_ours(args, rank, world):
         "plain_fp64": plain,
     }
     _leg("headline", out)
-    if not args.quick and not args.no_batch:
+    if not args.quick and not args.no_batch and solo:
         out["batch"] = run_batch(wl, rtol, atol, max(2, min(args.steps, 5)))
         _leg("batch", out)
-    if not args.quick and not args.no_rows:
+    if not args.quick and not args.no_rows and solo:
         out["composition"], out["aux_grid"], out["ordered_ridges"] = run_rows(wl, rtol, atol)
         _leg("composition", out)
     if not args.no_e2e and not args.quick:
@@ -569,7 +575,7 @@ def run_ours(args, rank, world):
         out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value,
                                                truth=truth)
         _leg("cpu_baseline", out)
-    if not args.quick and not args.no_configs:
+    if not args.quick and not args.no_configs and solo:
         cpu = rank == 0 and not args.no_cpu_baseline
         out["c0_double_gyre"] = run_c0(cpu=cpu)
         _leg("c0_double_gyre", out)
