@@ -70,6 +70,12 @@ int validate_flow(const nbcs_flow* flow, const double* params, int32_t np, int p
             return set_error(NBCS_ERR_UNSUPPORTED,
                              "mixed precision: spline grids of 2^32 nodes or more (with the "
                              "2-node border) are not supported; use precision fp64");
+        // the FP32 cell search takes the cell index from the float mantissa
+        for (int d = 0; d < 3 && precision == NBCS_PREC_MIXED; ++d)
+            if (flow->grid[3 * d + 2] > 8388608.0)
+                return set_error(NBCS_ERR_UNSUPPORTED,
+                                 "mixed precision: spline grid axis %d has more than 2^23 nodes; "
+                                 "use precision fp64", d);
         break;
     }
     default:

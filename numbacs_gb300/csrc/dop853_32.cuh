@@ -133,17 +133,15 @@ __device__ __forceinline__ float f2_minus(F2 a, F2 b)  // (a - b) rounded to flo
 // Terms j >= J of the stage argument combination sum_{j<S} a_Sj k_j: the
 // nonzero ones only, in ascending j.  KS is the stride of the shared-memory
 // column of stage derivatives (the block size).
+// The (x, y) halves of k_j share the coefficient: one paired FMA per term
+// (fma_pair, bit-identical to two fmaf).
 template <int S, int KS, int J = 0>
-__device__ __forceinline__ void stage_terms(const float2* kc, float& x, float& y)
+__device__ __forceinline__ void stage_terms(const float2* kc, float2& xy)
 {
     if constexpr (J < S) {
         constexpr float a = DP853F::a(S, J);
-        if constexpr (a != 0.f) {
-            const float2 kj = kc[J * KS];
-            x = fmaf(a, kj.x, x);
-            y = fmaf(a, kj.y, y);
-        }
-        stage_terms<S, KS, J + 1>(kc, x, y);
+        if constexpr (a != 0.f) xy = fma_pair(a, kc[J * KS], xy);
+        stage_terms<S, KS, J + 1>(kc, xy);
     }
 }
 
@@ -151,34 +149,25 @@ __device__ __forceinline__ void stage_terms(const float2* kc, float& x, float& y
 template <int S, int KS>
 __device__ __forceinline__ void stage_combo(const float2* kc, float* a0, float* a1, float* c)
 {
-    float x = 0.f, y = 0.f;
-    stage_terms<S, KS>(kc, x, y);
-    *a0 = x;
-    *a1 = y;
+    float2 xy = make_float2(0.f, 0.f);
+    stage_terms<S, KS>(kc, xy);
+    *a0 = xy.x;
+    *a1 = xy.y;
     *c = dp853_c32(S);
 }
 
 // The step's solution increment sum b_j k_j and the two error estimates
 // sum e5_j k_j, sum e3_j k_j, over the stages with a nonzero weight.
 template <int KS, int J = 0>
-__device__ __forceinline__ void step_sums(const float2* kc, float* b, float* e5, float* e3)
+__device__ __forceinline__ void step_sums(const float2* kc, float2& b, float2& e5, float2& e3)
 {
     if constexpr (J < 12) {
         constexpr float wb = DP853F::b(J), w5 = DP853F::e5(J), w3 = DP853F::e3(J);
         if constexpr (wb != 0.f || w5 != 0.f || w3 != 0.f) {
             const float2 kj = kc[J * KS];
-            if constexpr (wb != 0.f) {
-                b[0] = fmaf(wb, kj.x, b[0]);
-                b[1] = fmaf(wb, kj.y, b[1]);
-            }
-            if constexpr (w5 != 0.f) {
-                e5[0] = fmaf(w5, kj.x, e5[0]);
-                e5[1] = fmaf(w5, kj.y, e5[1]);
-            }
-            if constexpr (w3 != 0.f) {
-                e3[0] = fmaf(w3, kj.x, e3[0]);
-                e3[1] = fmaf(w3, kj.y, e3[1]);
-            }
+            if constexpr (wb != 0.f) b = fma_pair(wb, kj, b);
+            if constexpr (w5 != 0.f) e5 = fma_pair(w5, kj, e5);
+            if constexpr (w3 != 0.f) e3 = fma_pair(w3, kj, e3);
         }
         step_sums<KS, J + 1>(kc, b, e5, e3);
     }
@@ -290,8 +279,9 @@ __device__ int dop853_solve32(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F
         }
         fsal = false;
         *nfcn += 11;
-        float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
-        step_sums<KS>(kc, b, e5, e3);
+        float2 b2 = make_float2(0.f, 0.f), e52 = b2, e32 = b2;
+        step_sums<KS>(kc, b2, e52, e32);
+        const float b[2] = {b2.x, b2.y}, e5[2] = {e52.x, e52.y}, e3[2] = {e32.x, e32.y};
         F2 ynew[2];
         float err = 0.f, err2 = 0.f;
 #pragma unroll

@@ -163,8 +163,12 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
     float u = ((vh + vs) - A.a_h) * A.dinv;
     // NaN needs no branch: fmaxf picks cell 0 and the offset below is NaN
     const float top = (float)(A.n - 2);
-    int i = (int)floorf(fminf(fmaxf(u, 0.0f), top));
-    float fi = (float)i;
+    // floor of uc in [0, n - 2] (below 2^23) by the magic-number method:
+    // adding 2^23 rounded toward -inf leaves 2^23 + floor(uc), whose low
+    // mantissa bits are the cell index (full-rate adds instead of conversions)
+    const float fl = __fadd_rd(fminf(fmaxf(u, 0.0f), top), 8388608.0f);
+    const int i = __float_as_int(fl) - 0x4B000000;
+    const float fi = fl - 8388608.0f;  // exact
     float s, lo;
     if (EXACT) {  // the node is a float: one FMA (same result as the sum below)
         s = fmaf(fi, A.d_h, A.a_h);
@@ -179,22 +183,26 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
         float err = __fadd_rn(__fsub_rn(A.a_h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
         lo = err + (e + A.a_l);
     }
-    float r = __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
+    // vs - 0 is vs exactly: the exact-node form subtracts nothing
+    float r = EXACT ? __fadd_rn(__fsub_rn(vh, s), vs) : __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
     *t = r * A.dinv;
-    if (i == 0) {
-        const float ex = __fadd_rn(__fsub_rn(vh, A.a_h), __fsub_rn(vs, A.a_l));
-        if (ex < 0.0f) {
-            *outside = true;
-            if (XM != 0) *t = 0.0f;
-            if (XM == 2) *dl = ex * A.dinv;
+    // one test for both end cells (i = 0 or n - 2): interior cells skip it
+    if ((unsigned)(i - 1) >= (unsigned)(A.n - 3)) {
+        if (i == 0) {
+            const float ex = __fadd_rn(__fsub_rn(vh, A.a_h), __fsub_rn(vs, A.a_l));
+            if (ex < 0.0f) {
+                *outside = true;
+                if (XM != 0) *t = 0.0f;
+                if (XM == 2) *dl = ex * A.dinv;
+            }
         }
-    }
-    if (i == A.n - 2) {  // not "else": on a 2-node axis cell 0 holds both ends
-        const float ex = __fadd_rn(__fsub_rn(vh, A.b_h), __fsub_rn(vs, A.b_l));
-        if (ex > 0.0f) {
-            *outside = true;
-            if (XM != 0) *t = 1.0f;
-            if (XM == 2) *dl = ex * A.dinv;
+        if (i == A.n - 2) {  // not "else": on a 2-node axis cell 0 holds both ends
+            const float ex = __fadd_rn(__fsub_rn(vh, A.b_h), __fsub_rn(vs, A.b_l));
+            if (ex > 0.0f) {
+                *outside = true;
+                if (XM != 0) *t = 1.0f;
+                if (XM == 2) *dl = ex * A.dinv;
+            }
         }
     }
     return i;
@@ -255,6 +263,14 @@ __device__ __forceinline__ void spline_row32(const SplineGridF& g, const float* 
     }
 }
 
+// w * (a.x, a.y) + (c.x, c.y) as one paired FP32 FMA (fma.rn.f32x2, sm_100 and
+// later): each half rounds exactly as fmaf does, so a sum built from these is
+// bit-identical to the same sum of scalar fmaf calls in the same order.
+__device__ __forceinline__ float2 fma_pair(float w, float2 a, float2 c)
+{
+    return __ffma2_rn(make_float2(w, w), a, c);
+}
+
 template <int LP>
 __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const float* __restrict__ c,
                                                  int it, int ix, int iy, float ft, const float* wx,
@@ -265,7 +281,9 @@ __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const flo
     const int a0 = S::first_level(q);  // first time level
     float wt4[4];
     bspline_w32(ft, wt4);
-    float au = 0.0f, av = 0.0f;
+    // (u, v) contracted together: the quad layout interleaves u and v, so the
+    // two halves of every tap are one register pair and one paired FMA
+    float2 acc = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int r = 0; r < S::kLevels; ++r) {
         const int a = a0 + r;
@@ -273,30 +291,29 @@ __device__ __forceinline__ void spline_eval_uv32(const SplineGridF& g, const flo
         // quad-entry index in 32 bits (flows with 2^32 entries or more are refused)
         const unsigned e0 = (unsigned)(it + a) * (unsigned)g.st + (unsigned)ix * (unsigned)g.sx +
                             (unsigned)iy;
-        float su = 0.0f, sv = 0.0f;
+        float2 s = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             float p[8];
             spline_row32(g, c, e0 + (unsigned)b * (unsigned)g.sx, p);
-            const float bu = fmaf(wy[0], p[0], fmaf(wy[1], p[2], fmaf(wy[2], p[4], wy[3] * p[6])));
-            const float bv = fmaf(wy[0], p[1], fmaf(wy[1], p[3], fmaf(wy[2], p[5], wy[3] * p[7])));
-            su = fmaf(wx[b], bu, su);
-            sv = fmaf(wx[b], bv, sv);
+            float2 bb = __fmul2_rn(make_float2(wy[3], wy[3]), make_float2(p[6], p[7]));
+            bb = fma_pair(wy[2], make_float2(p[4], p[5]), bb);
+            bb = fma_pair(wy[1], make_float2(p[2], p[3]), bb);
+            bb = fma_pair(wy[0], make_float2(p[0], p[1]), bb);
+            s = fma_pair(wx[b], bb, s);
         }
-        au = fmaf(wt, su, au);
-        av = fmaf(wt, sv, av);
+        acc = fma_pair(wt, s, acc);
     }
     if (LP > 1) {
         const unsigned lane = threadIdx.x & 31u;
         const unsigned gmask = ((1u << LP) - 1u) << (lane & ~(unsigned)(LP - 1));
 #pragma unroll
-        for (int o = 1; o < LP; o <<= 1) {
-            au += __shfl_xor_sync(gmask, au, o);
-            av += __shfl_xor_sync(gmask, av, o);
-        }
+        for (int o = 1; o < LP; o <<= 1)
+            acc = __fadd2_rn(acc, make_float2(__shfl_xor_sync(gmask, acc.x, o),
+                                              __shfl_xor_sync(gmask, acc.y, o)));
     }
-    *u = au;
-    *v = av;
+    *u = acc.x;
+    *v = acc.y;
 }
 
 // derivative of the cubic B-spline basis with respect to the cell offset t

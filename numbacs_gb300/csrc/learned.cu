@@ -185,8 +185,9 @@ __device__ void solve32_warp(const Flow& fl, const ParamsF& P, F2 x, F2 xend, F2
             kc[s * kThreads32] = make_float2(kk[0], kk[1]);
         }
         *nfcn += 11;
-        float b[2] = {0.f, 0.f}, e5[2] = {0.f, 0.f}, e3[2] = {0.f, 0.f};
-        step_sums<kThreads32>(kc, b, e5, e3);
+        float2 b2 = make_float2(0.f, 0.f), e52 = b2, e32 = b2;
+        step_sums<kThreads32>(kc, b2, e52, e32);
+        const float b[2] = {b2.x, b2.y}, e5[2] = {e52.x, e52.y}, e3[2] = {e32.x, e32.y};
         F2 ynew[2];
         float err = 0.f, err2 = 0.f;
 #pragma unroll
