@@ -62,6 +62,11 @@ def test_invalid_arguments_are_reported_without_a_gpu():
     rc = L.nbcs_flowmap_grid_2d(f, 0.0, 1.0, None, 1, None, 1, p.ctypes.data_as(_lib._vp), 1,
                                 1e-6, 1e-8, None, None, None, opts, None)
     assert rc == -4 and b"2^32" in L.nbcs_last_error()
+    # ... and takes cell indices from float mantissas: at most 2^23 nodes per axis
+    f.grid[:] = [0.0, 1.0, 3.0, 0.0, 1.0, 3.0, 0.0, 1.0, 9000000.0]
+    rc = L.nbcs_flowmap_grid_2d(f, 0.0, 1.0, None, 1, None, 1, p.ctypes.data_as(_lib._vp), 1,
+                                1e-6, 1e-8, None, None, None, opts, None)
+    assert rc == -4 and b"2^23" in L.nbcs_last_error()
     assert L.nbcs_percentile(None, 0, 50.0, None, None, 0, None) == -1
 
 
