@@ -546,6 +546,9 @@ def run_ours(args, rank, world):
                                        "count DRAM bytes" % ("flowmap32_geo.md" if prec == "mixed"
                                                              else "flowmap64_geo.md"),
                      "peak_source": "in-run FMA probe (nbcs_probe_fma), burst",
+                     # what actually bounds the kernel (it gathers, it does not
+                     # stream): the busiest unit of the same ncu capture
+                     "limiter_from_profile": _profile_line(prec, "limiter"),
                      "kernel": "flowmap32_kernel" if prec == "mixed" else "flowmap64_kernel",
                      "flops_per_launch": flops_launch, "launch_ms": fm_ms,
                      "gather": {"bytes_per_launch": gather_b,
@@ -926,17 +929,23 @@ def run_c0(steps=5, cpu=True):
     return out
 
 
-def _profile_traffic(prec):
-    """DRAM bytes per launch of the integrator from the committed ncu summary."""
+def _profile_line(prec, key):
+    """The text after `key:` in the committed ncu summary of the integrator."""
     name = "flowmap32_geo.md" if prec == "mixed" else "flowmap64_geo.md"
     path = os.path.join(ROOT, "profiles", name)
     try:
         for ln in open(path):
-            if ln.startswith("dram_bytes_per_launch:"):
-                return float(ln.split(":", 1)[1].split()[0])
+            if ln.startswith(key + ":"):
+                return ln.split(":", 1)[1].strip()
     except OSError:
         pass
     return None
+
+
+def _profile_traffic(prec):
+    """DRAM bytes per launch of the integrator from the committed ncu summary."""
+    v = _profile_line(prec, "dram_bytes_per_launch")
+    return float(v.split()[0]) if v else None
 
 
 def _hbm_peak():
