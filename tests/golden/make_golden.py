@@ -24,6 +24,10 @@ imported here because numba / numbalsoda / interpolation are absent):
   tests/test_flows.py literals      spline coefficients Cu/Cv (:74-133), spline values at 27
                                     points (:208-229), double-gyre and Bickley velocities
                                     at the same 27 points (:315-357)
+  tests/test_utils.py literals      the deformation-gradient stencils at grid point (5, 5):
+                                    gradF_stencil_2D of fm (:74-89), gradF_aux_stencil_2D and
+                                    gradF_main_stencil_2D of fm_aux (:91-120), and
+                                    eigvalsh_max_2D of B^T B (:190-199)
 
 The ``.npy`` files are read with ``allow_pickle=False``; the ``.pkl`` file is read
 with an unpickler that only admits numpy array reconstruction; the test-source
@@ -83,7 +87,7 @@ def _test_literals(path):
         for node in ast.walk(fn):
             if (isinstance(node, ast.Assign) and len(node.targets) == 1
                     and isinstance(node.targets[0], ast.Name)
-                    and node.targets[0].id.endswith("_expected")):
+                    and (node.targets[0].id.endswith("_expected") or node.targets[0].id == "B")):
                 try:
                     out[(fn.name, node.targets[0].id)] = _eval_literal(node.value)
                 except (ValueError, SyntaxError):
@@ -114,6 +118,12 @@ def main(ref_root):
     arrays["dg_vel"] = np.stack([du, dv], axis=1)
     bu, bv = lit[("test_get_predefined_callable_bickley", "veli_expected")]
     arrays["bickley_vel"] = np.stack([bu, bv], axis=1)
+    ut = _test_literals(os.path.join(ref_root, "tests", "test_utils.py"))
+    arrays["gradF_55"] = np.array(ut[("test_gradF_stencil_2D", "gradF_expected")])
+    arrays["gradF_aux_55"] = np.array(ut[("test_gradF_aux_stencil_2D", "gradF_aux_expected")])
+    arrays["gradF_main_55"] = np.array(ut[("test_gradF_main_stencil_2D", "gradF_main_expected")])
+    arrays["eigvalsh_B"] = np.asarray(ut[("test_eigvalsh_max_2D", "B")], dtype=np.float64)
+    arrays["eigvalsh_max"] = np.array(ut[("test_eigvalsh_max_2D", "eigval_expected")])
     out = os.path.join(HERE, "reference_fixtures.npz")
     np.savez_compressed(out, **arrays)
     for k, v in sorted(arrays.items()):

@@ -258,3 +258,10 @@ def test_ordered_ridges_match_oracle_fed(nb, orc, pct):
     assert len(ridges) == len(ref) and len(ref) > 0
     for a, b in zip(ridges, ref):
         assert np.array_equal(a, b)
+
+
+def test_stencil_golden_literals_gpu(nb, golden, coords_dg):
+    """The reference's stencil literals (tests/test_utils.py) through the GPU
+    C_eig_2D / C_eig_aux_2D kernels (the checks of test_oracle_golden.py)."""
+    from test_oracle_golden import stencil_literal_checks
+    stencil_literal_checks(nb.C_eig_2D, nb.C_eig_aux_2D, golden, coords_dg)

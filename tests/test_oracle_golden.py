@@ -399,3 +399,46 @@ def test_ordered_ridges_native_buffers(orc, golden, coords_dg):
     assert n_pts.value == sum(golden["ordered_%d" % k].shape[0] for k in range(n_r.value))
     rc = L.nbcs_order_ridges(*args, None, 0, None, 0, None, None)
     assert rc == -1
+
+
+def _cauchy_green(g):
+    """C = F^T F from the stencil tuple (dFx/dx, dFx/dy, dFy/dx, dFy/dy), as the
+    reference assembles it (diagnostics.py:161-175)."""
+    a, b, c, d = g
+    off = a * b + c * d
+    return np.array([[a * a + c * c, off], [off, b * b + d * d]])
+
+
+def stencil_literal_checks(C_eig_2D, C_eig_aux_2D, golden, coords_dg):
+    """The reference's stencil literals (tests/test_utils.py:74-120, 190-199)
+    through the Cauchy-Green eigen-solvers: C at grid point (5, 5) of fm.npy and
+    fm_aux.npy, and eigvalsh_max_2D of B^T B via a linear flow map."""
+    x, y = coords_dg
+    dx, dy = x[1], y[1]
+    fm = golden["fm"].astype(np.float64)
+    ev, vec = (np.asarray(a) for a in C_eig_2D(fm, dx, dy))
+    C = vec[5, 5] @ np.diag(ev[5, 5]) @ vec[5, 5].T
+    assert np.allclose(C, _cauchy_green(golden["gradF_55"]))
+    fa = golden["fm_aux"].astype(np.float64)
+    ev, vec = (np.asarray(a) for a in C_eig_aux_2D(fa, dx, dy, 1e-5))
+    # eig_main: eigenvalues of the main-grid C, eigenvectors of the +-h C
+    assert np.allclose(ev[5, 5], np.linalg.eigvalsh(_cauchy_green(golden["gradF_main_55"])))
+    _, v_aux = np.linalg.eigh(_cauchy_green(golden["gradF_aux_55"]))
+    assert np.allclose(np.abs(np.sum(vec[5, 5] * v_aux, axis=0)), 1.0)
+    ev4, vec4 = (np.asarray(a) for a in C_eig_aux_2D(np.ascontiguousarray(fa[:, :, :4]), dx, dy,
+                                                       1e-5, eig_main=False))
+    C4 = vec4[5, 5] @ np.diag(ev4[5, 5]) @ vec4[5, 5].T
+    assert np.allclose(C4, _cauchy_green(golden["gradF_aux_55"]))
+    # a linear flow map F(x, y) = B (x, y): central differences give F = B exactly
+    # up to rounding, so lambda_max(C) is eigvalsh_max_2D(B^T B)
+    B = golden["eigvalsh_B"]
+    xg, yg = np.linspace(0.0, 1.0, 7), np.linspace(0.0, 2.0, 9)
+    X, Y = np.meshgrid(xg, yg, indexing="ij")
+    lin = np.stack([B[0, 0] * X + B[0, 1] * Y, B[1, 0] * X + B[1, 1] * Y], axis=-1)
+    ev, _ = (np.asarray(a) for a in C_eig_2D(lin, xg[1], yg[1]))
+    lmax = ev[1:-1, 1:-1, 1]
+    assert np.allclose(lmax, float(golden["eigvalsh_max"]), rtol=1e-12, atol=0)
+
+
+def test_stencil_golden_literals(orc, golden, coords_dg):
+    stencil_literal_checks(orc.C_eig_2D, orc.C_eig_aux_2D, golden, coords_dg)
