@@ -116,3 +116,30 @@ def test_geo_workload_shapes():
     assert len(kx) == 256
     kmag = np.hypot(kx, ky)
     assert kmag.min() >= 2 * np.pi / 5000 and kmag.max() <= 2 * np.pi / 100
+
+
+def test_fails_loudly_without_library(tmp_path):
+    """No CPU fallback: with the CUDA library absent the package raises on load
+    and on a compute call (run in a child so the session's loaded handle stays)."""
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np\n"
+        "import numbacs_gb300 as nb\n"
+        "from numbacs_gb300 import _lib\n"
+        "try:\n"
+        "    _lib.load()\n"
+        "    raise SystemExit('load() did not raise')\n"
+        "except RuntimeError as e:\n"
+        "    assert 'not built' in str(e), e\n"
+        "fl, p, _ = nb.get_predefined_flow('double_gyre')\n"
+        "try:\n"
+        "    nb.flowmap_grid_2D(fl, 0.0, 1.0, np.linspace(0, 2, 5), np.linspace(0, 1, 3), p)\n"
+        "    raise SystemExit('flowmap_grid_2D did not raise')\n"
+        "except RuntimeError:\n"
+        "    pass\n"
+        "print('loud')\n")
+    env = dict(os.environ, NBCS_LIB=str(tmp_path / "missing" / "libnbcs.so"))
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0 and "loud" in r.stdout, r.stderr[-2000:]
