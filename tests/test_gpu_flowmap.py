@@ -314,3 +314,46 @@ def test_mixed_precision_non_dyadic_grid(nb):
     ep, em = _err_stats(plain, truth), _err_stats(mixed, truth)
     assert em["median"] <= 3 * ep["median"] + 1e-9, (em, ep)
     assert em["q99"] <= 3 * ep["q99"] + 1e-8, (em, ep)
+
+
+def test_status_nan_spline_coefficients(nb, orc):
+    """Host-injected fault: one NaN velocity sample.  The natural-BC prefilter
+    couples whole lines, so every coefficient turns NaN; particles that start
+    inside the grid box return NONFINITE (-4), those outside (zero velocity)
+    return OK -- on both paths, as the oracle does, with no hang or fault.
+    The batched kernels report the same codes, and MAX_STEPS (-2) under a
+    one-step limit (as the oracle does: even a particle at rest needs many
+    growing steps to cover 18 h)."""
+    from numbacs_gb300.batch import FTLEBatch, Field
+    tv, lon, lat = np.arange(9) * 3.0, np.linspace(-20.0, 20.0, 11), np.linspace(0.0, 30.0, 9)
+    T3, X3, Y3 = np.meshgrid(tv, lon, lat, indexing="ij")
+    U = 30.0 * np.sin(0.15 * X3 + 0.05 * T3) * np.cos(0.1 * Y3)
+    V = 20.0 * np.cos(0.12 * X3) * np.sin(0.2 * Y3 - 0.03 * T3)
+    U[4, 5, 4] = np.nan
+    grid, Cu, Cv = nb.get_interp_arrays_2D(tv, lon, lat, U, V)
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    og, oCu, oCv = orc.get_interp_arrays_2D(tv, lon, lat, U, V)
+    ofl = orc.spline_flow(og, oCu, oCv, spherical=1)
+    xs, ys, p = np.linspace(-30.0, 30.0, 13), np.linspace(5.0, 25.0, 5), np.array([-1.0])
+    inside = np.abs(xs)[:, None] <= 20.0 + 0 * ys[None, :]
+    _, ost, _ = orc.flowmap_grid_2D(ofl, 24.0, -18.0, xs, ys, p, return_status=True)
+    assert np.array_equal(ost, np.where(inside, -4, 0))
+    for prec in ("fp64", "mixed"):
+        _, st = nb.flowmap_grid_2D(fl, 24.0, -18.0, xs, ys, p, return_status=True, precision=prec)
+        assert np.array_equal(st, ost), prec
+    for sched in (-1, -2, 2):
+        f = Field(fl, 24.0, -18.0, xs, ys, p)
+        FTLEBatch([f], precision="mixed", blocks_per_sm=sched, graph=False).run()
+        assert np.array_equal(f.status.cpu().numpy(), ost), sched
+    # a one-step limit in the batch: MAX_STEPS where the oracle gives up too
+    U[4, 5, 4] = 1.0
+    grid, Cu, Cv = nb.get_interp_arrays_2D(tv, lon, lat, U, V)
+    fl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    og, oCu, oCv = orc.get_interp_arrays_2D(tv, lon, lat, U, V)
+    _, ost1, _ = orc.flowmap_grid_2D(orc.spline_flow(og, oCu, oCv, spherical=1), 24.0, -18.0, xs,
+                                     ys, p, nmax=1, return_status=True)
+    assert (ost1 == -2).all()
+    for sched in (-1, -2, 2):
+        f = Field(fl, 24.0, -18.0, xs, ys, p)
+        FTLEBatch([f], precision="mixed", blocks_per_sm=sched, graph=False, max_steps=1).run()
+        assert np.array_equal(f.status.cpu().numpy(), ost1), sched
