@@ -184,7 +184,8 @@ __device__ __forceinline__ int locate_pair(const AxisF& A, float vh, float vs, f
         lo = err + (e + A.a_l);
     }
     // vs - 0 is vs exactly: the exact-node form subtracts nothing
-    float r = EXACT ? __fadd_rn(__fsub_rn(vh, s), vs) : __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
+    float r = EXACT ? __fadd_rn(__fsub_rn(vh, s), vs)
+                    : __fadd_rn(__fsub_rn(vh, s), __fsub_rn(vs, lo));
     *t = r * A.dinv;
     // one test for both end cells (i = 0 or n - 2): interior cells skip it
     if ((unsigned)(i - 1) >= (unsigned)(A.n - 3)) {
