@@ -128,6 +128,15 @@ int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T,
                          const uint8_t* mask, double* flowmap, int32_t* status,
                          const nbcs_opts* opts, void* stream);
 
+/* flowmap (integration.py:8-62) and flowmap_grid_ND with ndims = 2
+ * (:186-247), method="dop853": the same integration for a list of points,
+ * pts (npts,2) C-order -> flowmap (npts,2); mask (npts,) u8 and status
+ * (npts,) int32 may be NULL; npts < 2^31; no step_model. */
+int nbcs_flowmap_pts(const nbcs_flow* flow, double t0, double T, const double* pts,
+                     int64_t npts, const double* params, int32_t np, double rtol, double atol,
+                     const uint8_t* mask, double* flowmap, int32_t* status,
+                     const nbcs_opts* opts, void* stream);
+
 /* flowmap_aux_grid_2D (integration.py:249-464) with method="dop853": every
  * grid point (x[i], y[j]) integrates the particles started at (x[i], y[j]) +
  * (h,0), (-h,0), (0,h), (0,-h) and, with eig_main, (0,0), into flowmap_aux

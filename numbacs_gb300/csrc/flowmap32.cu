@@ -44,6 +44,7 @@ flowmap32_kernel(Flow fl, ParamsF P, double ts, double te, const double* __restr
         int i, j;
         if (!tile_particle<LP, kFm32Block, kFm32TileJ>(t, nx, nyv, &i, &j)) continue;
         long k = (long)i * nyv + j;
+        if (!particle_exists(aux, k)) continue;  // uniform in a lane group
         double r0 = 0.0, r1 = 0.0, x0, y0;
         int st = NBCS_PARTICLE_MASKED, a = 0, rj = 0, nf = 0;
         if (particle_start(aux, x, y, mask, nx, i, j, &x0, &y0)) {

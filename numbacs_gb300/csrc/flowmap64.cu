@@ -34,6 +34,7 @@ flowmap64_kernel(Flow fl, Params P, double ts, double te, const double* __restri
         int i, j;
         if (!tile_particle<1, kFm64Block>(t, nx, nyv, &i, &j)) continue;
         const long k = (long)i * nyv + j;
+        if (!particle_exists(aux, k)) continue;
         double yv[2] = {0.0, 0.0}, x0, y0;
         int st = NBCS_PARTICLE_MASKED;
         Dop853Stats s = {0, 0, 0};
@@ -166,9 +167,25 @@ extern "C" int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T, 
                                     const nbcs_opts* opts, void* stream)
 {
     NBCS_RANGE();
-    const AuxGrid plain = {0, ny, 1, 0.0};
+    const AuxGrid plain = {0, ny, 1, 0.0, 0};
     return flowmap_particles(flow, t0, T, x, nx, y, ny, params, np, rtol, atol, mask, flowmap,
                              status, opts, stream, plain);
+}
+
+extern "C" int nbcs_flowmap_pts(const nbcs_flow* flow, double t0, double T, const double* pts,
+                                int64_t npts, const double* params, int32_t np, double rtol,
+                                double atol, const uint8_t* mask, double* flowmap, int32_t* status,
+                                const nbcs_opts* opts, void* stream)
+{
+    NBCS_RANGE();
+    if (npts < 0 || npts > 0x7fffffffL)
+        return set_error(NBCS_ERR_INVALID, "flowmap_pts: npts must be in [0, 2^31)");
+    if (opts && opts->step_model)
+        return set_error(NBCS_ERR_UNSUPPORTED, "flowmap_pts: no step_model");
+    const int W = kPointListColumns;
+    const AuxGrid list = {kPointList, W, 0, 0.0, (long)npts};
+    return flowmap_particles(flow, t0, T, pts, (int32_t)((npts + W - 1) / W), pts, W, params, np,
+                             rtol, atol, mask, flowmap, status, opts, stream, list);
 }
 
 extern "C" int nbcs_flowmap_aux_grid_2d(const nbcs_flow* flow, double t0, double T,
@@ -184,7 +201,7 @@ extern "C" int nbcs_flowmap_aux_grid_2d(const nbcs_flow* flow, double t0, double
         return set_error(NBCS_ERR_UNSUPPORTED, "aux grid: no step_model");
     if ((long)nx * ny * (eig_main ? 5 : 4) > 0x7fffffffL)
         return set_error(NBCS_ERR_INVALID, "aux grid: too many particles");
-    const AuxGrid aux = {eig_main ? 5 : 4, ny, compute_edge ? 1 : 0, h};
+    const AuxGrid aux = {eig_main ? 5 : 4, ny, compute_edge ? 1 : 0, h, 0};
     return flowmap_particles(flow, t0, T, x, nx, y, ny, params, np, rtol, atol, mask,
                              flowmap_aux, status, opts, stream, aux);
 }

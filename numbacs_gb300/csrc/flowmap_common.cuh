@@ -10,13 +10,28 @@ namespace nbcs {
 // (eig_main) or 4 particles per grid point, started at (x_i, y_j) + (h, 0),
 // (-h, 0), (0, h), (0, -h) [, (0, 0)] -- laid out as a virtual (nx, ny * n)
 // grid, so that the (nx, ny, n, 2) result is that grid's flow map and the
-// near-identical trajectories of one point sit in neighbouring lanes.
+// near-identical trajectories of one point sit in neighbouring lanes; or
+// (n = kPointList) the point list of flowmap (integration.py:8-62), npts
+// rows (x, y) of x, laid out as a virtual (ceil(npts / ny), ny) grid in list
+// order, so that consecutive points share a particle tile and the flat index
+// of entry (i, j) is the point index i * ny + j (entries past npts do not
+// exist: they are neither integrated nor written).
+constexpr int kPointList = -1;
+constexpr int kPointListColumns = 8;  // columns of the virtual grid of a point list
+
 struct AuxGrid {
-    int n;             // 0: plain grid; else 4 or 5 particles per grid point
-    int ny;            // columns of the real grid
+    int n;             // 0: plain grid; 4 or 5 particles per grid point; kPointList
+    int ny;            // columns of the real grid (of the virtual grid for a point list)
     int compute_edge;  // integrate the edge points (only their centre particle when n = 5)
     double h;
+    long npts;         // kPointList: number of points
 };
+
+// False for the padding entries of a point list's virtual grid.
+__device__ __forceinline__ bool particle_exists(const AuxGrid& A, long k)
+{
+    return A.n != kPointList || k < A.npts;
+}
 
 // Start point of particle (i, jv) of the virtual grid; false when it is masked
 // or skipped (its result stays 0 with status MASKED, as the reference leaves
@@ -30,6 +45,13 @@ __device__ __forceinline__ bool particle_start(const AuxGrid& A, const double* _
         if (mask && mask[(long)i * A.ny + jv]) return false;
         *x0 = x[i];
         *y0 = y[jv];
+        return true;
+    }
+    if (A.n == kPointList) {  // pts[k, :], k < npts (particle_exists)
+        const long k = (long)i * A.ny + jv;
+        if (mask && mask[k]) return false;
+        *x0 = x[2 * k];
+        *y0 = x[2 * k + 1];
         return true;
     }
     const int j = jv / A.n, k = jv - j * A.n;
@@ -59,7 +81,7 @@ struct FlowmapArgs {
     const void* step_model;
     cudaStream_t stream;
     // columns of the virtual particle grid
-    int nyv() const { return aux.n ? ny * aux.n : ny; }
+    int nyv() const { return aux.n > 0 ? ny * aux.n : ny; }
 };
 
 // Threads per block of the single-field integrator, and the width in y of the

@@ -1,7 +1,9 @@
 """Flow-map integration: the drop-in for numbacs.integration.flowmap_grid_2D,
-flowmap_aux_grid_2D and the flow-map composition functions.
+flowmap, flowmap_grid_ND, flowmap_aux_grid_2D and the flow-map composition
+functions.
 
-Reference: src/numbacs/integration.py:123-182 (flowmap_grid_2D), :249-464
+Reference: src/numbacs/integration.py:123-182 (flowmap_grid_2D), :8-62
+(flowmap), :186-247 (flowmap_grid_ND), :249-464
 (flowmap_aux_grid_2D), :609-737 (flowmap_composition, _initial, _step).  The
 reference loops over the particle grid with numba ``prange`` and calls
 numbalsoda's DOP853 per particle; here one CUDA thread (or lane group)
@@ -100,6 +102,62 @@ def flowmap_grid_2D(funcptr, t0, T, x, y, params, method="dop853", rtol=1e-6, at
     if return_stats:
         res.append(D.finish(stats, as_torch))
     return res[0] if len(res) == 1 else tuple(res)
+
+
+def flowmap(funcptr, t0, T, pts, params, method="dop853", rtol=1e-6, atol=1e-8, mask=None, *,
+            precision="fp64", max_steps=100000, return_status=False, return_stats=False):
+    """Flow map at t0+T of a list of points pts (npts, 2) -> (npts, 2)
+    (integration.py:8-62): the particles of flowmap_grid_2D, taken from a list
+    instead of a grid; mask (npts,) leaves entries 0.  Same keyword extras as
+    flowmap_grid_2D (no launch-shape knobs, no step_model)."""
+    if method.lower() != "dop853":
+        raise NotImplementedError("method=%r: only 'dop853' is implemented on the GPU" % method)
+    flow = _check_callable_flow(funcptr)
+    if precision not in _PREC:
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    D.require_cuda()
+    as_torch = D.is_torch(pts)
+    pd = D.to_dev(pts)
+    if pd.dim() != 2 or pd.shape[1] != 2:
+        raise ValueError("pts must have shape (npts, 2): the flows are two-dimensional")
+    npts = pd.shape[0]
+    md = D.mask_to_dev(mask)
+    if md is not None and tuple(md.shape) != (npts,):
+        raise ValueError("mask must have shape (npts,)")
+    prm = np.ascontiguousarray(
+        params.cpu().numpy() if isinstance(params, torch.Tensor) else params, dtype=np.float64)
+    out = D.empty((npts, 2))
+    status = D.empty((npts,), torch.int32)
+    stats = D.empty((npts, 3), torch.int32) if return_stats else None
+    opts = _lib.NbcsOpts()
+    opts.precision = _PREC[precision]
+    opts.max_steps = int(max_steps)
+    opts.stats = stats.data_ptr() if stats is not None else None
+    L = _lib.load()
+    _lib.check(L.nbcs_flowmap_pts(flow.struct, float(t0), float(T), D.ptr(pd), npts,
+                                  prm.ctypes.data_as(_lib._vp), len(prm), float(rtol), float(atol),
+                                  D.ptr(md), D.ptr(out), D.ptr(status), opts, D.stream_ptr()))
+    if not return_status and not as_torch:
+        _warn_unfinished("flowmap", status)
+    res = [D.finish(out, as_torch)]
+    if return_status:
+        res.append(D.finish(status, as_torch))
+    if return_stats:
+        res.append(D.finish(stats, as_torch))
+    return res[0] if len(res) == 1 else tuple(res)
+
+
+def flowmap_grid_ND(funcptr, t0, T, IC_flat, ndims, params, method="dop853", rtol=1e-6,
+                    atol=1e-8, **kwargs):
+    """flowmap_grid_ND (integration.py:186-247): the flow map of the initial
+    conditions IC_flat (npts * ndims,) -> (npts, ndims); the flows here are
+    two-dimensional, so ndims must be 2 (then it is flowmap of the rows)."""
+    if int(ndims) != 2:
+        raise ValueError("ndims must be 2: the flows are two-dimensional")
+    ic = IC_flat if isinstance(IC_flat, torch.Tensor) else np.asarray(IC_flat, dtype=np.float64)
+    if ic.shape[0] % 2:
+        raise ValueError("IC_flat length must be a multiple of ndims")
+    return flowmap(funcptr, t0, T, ic.reshape(-1, 2), params, method, rtol, atol, **kwargs)
 
 
 def flowmap_aux_grid_2D(funcptr, t0, T, x, y, params, h=1e-5, eig_main=True, compute_edge=True,

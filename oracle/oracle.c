@@ -487,6 +487,34 @@ int orc_flowmap_grid_2d(const orc_flow* fl, double t0, double T,
     return 0;
 }
 
+/* integration.py:8-62 (flowmap, method "dop853"): the same integration for
+ * a list of points pts (npts, 2); masked points are left 0. */
+int orc_flowmap_pts(const orc_flow* fl, double t0, double T, const double* pts, long npts,
+                    const double* params, double rtol, double atol, const uint8_t* mask,
+                    double* out, int32_t* status, int nmax, int nthreads)
+{
+    double ts = params[0] * t0;
+    double te = params[0] * (t0 + T);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (long k = 0; k < npts; ++k) {
+        if (mask && mask[k]) {
+            out[2 * k] = 0.0;
+            out[2 * k + 1] = 0.0;
+            if (status) status[k] = ORC_MASKED;
+            continue;
+        }
+        double yv[2] = {pts[2 * k], pts[2 * k + 1]};
+        int st = orc_dop853(fl, params, ts, te, yv, rtol, atol, nmax, 0);
+        out[2 * k] = yv[0];
+        out[2 * k + 1] = yv[1];
+        if (status) status[k] = st;
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------ FTLE */
 
 /* diagnostics.py:21-65 with utils.gradF_stencil_2D (:41-44) and

@@ -73,6 +73,11 @@ int orc_flowmap_grid_2d(const orc_flow* flow, double t0, double T,
                         const uint8_t* mask, double* out, int32_t* status,
                         int32_t* stats, int nmax, int nthreads);
 
+/* flowmap: pts (npts,2) -> out (npts,2); mask, status (npts,) nullable */
+int orc_flowmap_pts(const orc_flow* flow, double t0, double T, const double* pts, long npts,
+                    const double* params, double rtol, double atol, const uint8_t* mask,
+                    double* out, int32_t* status, int nmax, int nthreads);
+
 void orc_ftle_grid_2d(const double* fm, int nx, int ny, double T, double dx, double dy,
                       const uint8_t* mask, double* ftle);
 void orc_c_eig_2d(const double* fm, int nx, int ny, double dx, double dy,

@@ -2,6 +2,7 @@
 
 Every function mirrors one reference NumbaCS function on numpy arrays:
 
+  flowmap           src/numbacs/integration.py:8-62
   flowmap_grid_2D   src/numbacs/integration.py:123-182
   ftle_grid_2D      src/numbacs/diagnostics.py:21-65
   C_eig_2D          src/numbacs/diagnostics.py:200-244
@@ -72,6 +73,7 @@ def lib():
         L.orc_eval_spline_3d.argtypes = [vp, vp, i, d, d, d]
         L.orc_eval_spline_3d.restype = d
         L.orc_flowmap_grid_2d.argtypes = [vp, d, d, vp, i, vp, i, vp, i, d, d, vp, vp, vp, vp, i, i]
+        L.orc_flowmap_pts.argtypes = [vp, d, d, vp, ctypes.c_long, vp, d, d, vp, vp, vp, i, i]
         L.orc_ftle_grid_2d.argtypes = [vp, i, i, d, d, d, vp, vp]
         L.orc_c_eig_2d.argtypes = [vp, i, i, d, d, vp, vp, vp]
         L.orc_ftle_from_eig.argtypes = [vp, i64, d, vp]
@@ -176,6 +178,20 @@ def flowmap_grid_2D(flow, t0, T, x, y, params, rtol=1e-6, atol=1e-8, mask=None,
     if return_status:
         return out, status, stats
     return out
+
+
+def flowmap(flow, t0, T, pts, params, rtol=1e-6, atol=1e-8, mask=None, nmax=100000, nthreads=0,
+            return_status=False):
+    """integration.py:8-62 (method dop853): pts (npts, 2) -> (npts, 2)."""
+    pts = np.ascontiguousarray(pts, np.float64)
+    p = np.ascontiguousarray(params, np.float64)
+    npts = pts.shape[0]
+    out = np.zeros((npts, 2))
+    status = np.zeros(npts, np.int32)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib().orc_flowmap_pts(flow.ptr, float(t0), float(T), _dp(pts), npts, _dp(p), float(rtol),
+                          float(atol), _dp(m), _dp(out), _dp(status), int(nmax), int(nthreads))
+    return (out, status) if return_status else out
 
 
 def flowmap_aux_grid_2D(flow, t0, T, x, y, params, h=1e-5, eig_main=True, compute_edge=True,

@@ -357,3 +357,54 @@ def test_status_nan_spline_coefficients(nb, orc):
         f = Field(fl, 24.0, -18.0, xs, ys, p)
         FTLEBatch([f], precision="mixed", blocks_per_sm=sched, graph=False, max_steps=1).run()
         assert np.array_equal(f.status.cpu().numpy(), ost1), sched
+
+
+def test_flowmap_pts(nb, orc, golden, coords_dg, mask_dg):
+    """flowmap / flowmap_grid_ND (integration.py:8-62, :186-247): a point list
+    laid out 8 points to a row of a virtual grid; 231 points leave a partial
+    last row that is neither integrated nor written."""
+    x, y = coords_dg
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    pts = np.column_stack((X.ravel(), Y.ravel()))
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    fm = nb.flowmap(fl, 0.0, 8.0, pts, p)
+    assert fm.shape == (231, 2)
+    assert np.allclose(fm.reshape(21, 11, 2).astype(np.float32), golden["fm"])
+    # the same particles as the grid call, so the same bits
+    for prec in ("fp64", "mixed"):
+        g = nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p, precision=prec)
+        f = nb.flowmap(fl, 0.0, 8.0, pts, p, precision=prec)
+        assert np.array_equal(f.reshape(21, 11, 2), g), prec
+    fmm, st = nb.flowmap(fl, 0.0, 8.0, pts, p, mask=mask_dg.ravel(), return_status=True)
+    exp = golden["fm"].copy()
+    exp[mask_dg] = 0.0
+    assert np.allclose(fmm.reshape(21, 11, 2).astype(np.float32), exp)
+    assert np.array_equal(st == 1, mask_dg.ravel()) and (st[~mask_dg.ravel()] == 0).all()
+    assert np.array_equal(nb.flowmap_grid_ND(fl, 0.0, 8.0, pts.ravel(), 2, p), fm)
+    assert nb.flowmap(fl, 0.0, 8.0, np.zeros((0, 2)), p).shape == (0, 2)
+    # a spline flow on scattered points: FP64 bit-identical to the oracle, with
+    # identical statuses (points outside the grid box stay put)
+    tv, lon, lat = np.arange(9) * 3.0, np.linspace(-20.0, 20.0, 11), np.linspace(0.0, 30.0, 9)
+    T3, X3, Y3 = np.meshgrid(tv, lon, lat, indexing="ij")
+    U = 30.0 * np.sin(0.15 * X3 + 0.05 * T3) * np.cos(0.1 * Y3)
+    V = 20.0 * np.cos(0.12 * X3) * np.sin(0.2 * Y3 - 0.03 * T3)
+    grid, Cu, Cv = nb.get_interp_arrays_2D(tv, lon, lat, U, V)
+    sfl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    og, oCu, oCv = orc.get_interp_arrays_2D(tv, lon, lat, U, V)
+    ofl = orc.spline_flow(og, oCu, oCv, spherical=1)
+    rng = np.random.default_rng(3)
+    sp = np.column_stack((rng.uniform(-25.0, 25.0, 1003), rng.uniform(-2.0, 32.0, 1003)))
+    sm = rng.random(1003) < 0.1
+    ps = np.array([-1.0])
+    f64, s64 = nb.flowmap(sfl, 24.0, -18.0, sp, ps, mask=sm, return_status=True)
+    of, ost = orc.flowmap(ofl, 24.0, -18.0, sp, ps, mask=sm, return_status=True)
+    assert np.array_equal(f64, of) and np.array_equal(s64, ost)
+    f32 = nb.flowmap(sfl, 24.0, -18.0, sp, ps, mask=sm, precision="mixed")
+    # mixed against FP64 at the default rtol: FP32-stage noise, except where a
+    # trajectory grazes the box edge and the two leave it at different times
+    e = np.abs(f32 - of).max(-1)
+    assert np.median(e) <= 1e-5 and np.quantile(e, 0.99) <= 1e-3, (np.median(e), e.max())
+    # torch in, torch out, on the device
+    tp = torch.from_numpy(sp).cuda()
+    ft = nb.flowmap(sfl, 24.0, -18.0, tp, ps, mask=torch.from_numpy(sm).cuda())
+    assert ft.is_cuda and torch.equal(ft.cpu(), torch.from_numpy(f64))

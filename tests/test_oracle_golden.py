@@ -442,3 +442,21 @@ def stencil_literal_checks(C_eig_2D, C_eig_aux_2D, golden, coords_dg):
 
 def test_stencil_golden_literals(orc, golden, coords_dg):
     stencil_literal_checks(orc.C_eig_2D, orc.C_eig_aux_2D, golden, coords_dg)
+
+
+def test_flowmap_pts_golden(orc, golden, coords_dg, mask_dg):
+    """flowmap on the grid's points (tests/test_integration.py:37-41), plain
+    and masked (a mask over the points leaves their rows 0)."""
+    x, y = coords_dg
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    pts = np.column_stack((X.ravel(), Y.ravel()))
+    dg = orc.double_gyre()
+    p = np.array([1.0, 0.1, 0.25, 0.0, 0.2 * np.pi, 0.0])
+    fm = orc.flowmap(dg, 0.0, 8.0, pts, p).reshape(len(x), len(y), 2)
+    assert np.allclose(fm.astype(np.float32), golden["fm"])
+    assert np.array_equal(fm, orc.flowmap_grid_2D(dg, 0.0, 8.0, x, y, p))
+    fmm, st = orc.flowmap(dg, 0.0, 8.0, pts, p, mask=mask_dg.ravel(), return_status=True)
+    exp = golden["fm"].copy()
+    exp[mask_dg] = 0.0
+    assert np.allclose(fmm.reshape(len(x), len(y), 2).astype(np.float32), exp)
+    assert np.array_equal(st == 1, mask_dg.ravel())
