@@ -32,7 +32,10 @@ _PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
 class Field:
     """One FTLE field: the arguments of one flowmap_grid_2D call plus FTLE."""
 
-    def __init__(self, flow, t0, T, x, y, params, rtol=1e-6, atol=1e-8, mask=None, ftle=True):
+    def __init__(self, flow, t0, T, x, y, params, rtol=1e-6, atol=1e-8, mask=None, ftle=True,
+                 out=None):
+        """``out``: an optional contiguous float64 (nx, ny, 2) CUDA tensor that
+        receives the flow map (e.g. one slice of a stack of maps)."""
         self.flow = _check_callable_flow(flow)
         self.t0, self.T = float(t0), float(T)
         self.x, self.y = D.to_dev(x), D.to_dev(y)
@@ -44,14 +47,23 @@ class Field:
         self.mask = D.mask_to_dev(mask)
         self.want_ftle = bool(ftle)
         nx, ny = self.x.numel(), self.y.numel()
-        self.flowmap = D.empty((nx, ny, 2))
+        if out is None:
+            self.flowmap = D.empty((nx, ny, 2))
+        elif (tuple(out.shape) != (nx, ny, 2) or out.dtype != torch.float64 or not out.is_cuda
+              or not out.is_contiguous()):
+            raise ValueError("out must be a contiguous float64 (nx, ny, 2) CUDA tensor")
+        else:
+            self.flowmap = out
         self.status = D.empty((nx, ny), torch.int32)
         self.ftle = D.empty((nx, ny)) if ftle else None
         self.evec = D.empty((nx, ny, 2)) if ftle else None
-        xs = self.x.cpu()
-        ys = self.y.cpu()
-        self.dx = float(xs[1] - xs[0]) if nx > 1 else 1.0
-        self.dy = float(ys[1] - ys[0]) if ny > 1 else 1.0
+        # the grid spacing only enters the FTLE (read on the host: a sync)
+        self.dx = self.dy = 1.0
+        if ftle:
+            xs = self.x.cpu()
+            ys = self.y.cpu()
+            self.dx = float(xs[1] - xs[0]) if nx > 1 else 1.0
+            self.dy = float(ys[1] - ys[0]) if ny > 1 else 1.0
 
     @property
     def particles(self):
