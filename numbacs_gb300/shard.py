@@ -33,6 +33,50 @@ import numpy as np
 HALO = 2
 
 
+def _all_gather_rows(a, group=None):
+    """Every rank's array ``a`` (equal trailing shape, any number of rows),
+    gathered in rank order with tensor collectives: the row counts, then the
+    rows padded to the longest block.  CUDA tensors under NCCL, host tensors
+    otherwise (gloo)."""
+    import torch
+    import torch.distributed as dist
+    dev = (torch.device("cuda", torch.cuda.current_device())
+           if dist.get_backend(group) == "nccl" else torch.device("cpu"))
+    a = np.ascontiguousarray(a)
+    world = dist.get_world_size(group)
+    n = torch.tensor([a.shape[0]], dtype=torch.int64, device=dev)
+    counts = [torch.empty_like(n) for _ in range(world)]
+    dist.all_gather(counts, n, group=group)
+    counts = [int(c.item()) for c in counts]
+    buf = torch.zeros((max(counts),) + a.shape[1:], dtype=torch.from_numpy(a).dtype, device=dev)
+    buf[:a.shape[0]] = torch.from_numpy(a).to(dev)
+    outs = [torch.empty_like(buf) for _ in range(world)]
+    dist.all_gather(outs, buf, group=group)
+    return [o[:c].cpu().numpy() for o, c in zip(outs, counts)]
+
+
+def _gather_parts(part, group=None):
+    """block_ridges of every rank, in rank order: each rank's components flattened
+    to arrays (sizes, pixel indices, points) and its boundary rows, gathered
+    with _all_gather_rows, then rebuilt."""
+    comps = part["comps"]
+    sizes = np.array([len(c[0]) for c in comps], np.int64)
+    idx = np.concatenate([c[0] for c in comps]) if comps else np.zeros(0, np.int64)
+    pts = np.concatenate([c[1] for c in comps]) if comps else np.zeros((0, 2))
+    meta = np.array([part["rows"][0], part["rows"][1], part["ny"]], np.int64)
+    edges = np.stack([np.asarray(part["top"], np.int64), np.asarray(part["bottom"], np.int64)])
+    g = [_all_gather_rows(v, group) for v in (meta, sizes, idx.astype(np.int64),
+                                              np.asarray(pts, np.float64), edges)]
+    parts = []
+    for meta_r, sizes_r, idx_r, pts_r, edges_r in zip(*g):
+        cut = np.cumsum(np.concatenate([[0], sizes_r]))
+        parts.append({"rows": (int(meta_r[0]), int(meta_r[1])), "ny": int(meta_r[2]),
+                      "comps": [(idx_r[cut[k]:cut[k + 1]], pts_r[cut[k]:cut[k + 1]])
+                                for k in range(len(sizes_r))],
+                      "top": edges_r[0], "bottom": edges_r[1]})
+    return parts
+
+
 def row_blocks(nx, world):
     """Owned rows [i0, i1) of each rank: contiguous, in rank order, sizes
     differing by at most one."""
@@ -119,8 +163,9 @@ def sharded_ftle_ridge_pts(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile
     """ftle_ridge_pts of the field's flow map, computed by every rank of the
     process group on its row block; every rank returns the full (k, 2) numpy
     array of ridge points, identical to the one-GPU pipeline
-    flowmap_grid_2D -> ftle_evec_2D -> ftle_ridge_pts.  Collectives: two
-    all_gather_object calls on the host (owned FTLE rows, ridge points)."""
+    flowmap_grid_2D -> ftle_evec_2D -> ftle_ridge_pts.  Collectives: tensor
+    all_gathers of the owned FTLE rows and of the ridge points (each after a
+    gather of the row counts)."""
     import torch.distributed as dist
     ops = ops or GpuOps()
     if dist.is_available() and dist.is_initialized():
@@ -128,18 +173,12 @@ def sharded_ftle_ridge_pts(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile
     else:
         rank, world = 0, 1
     state, owned = block_ftle(ops, rank, world, flow, t0, T, x, y, params, **flowmap_kw)
-    if world == 1:
-        rows = [owned]
-    else:
-        rows = [None] * world
-        dist.all_gather_object(rows, owned, group=group)
+    rows = [owned] if world == 1 else _all_gather_rows(np.asarray(owned, np.float64), group)
     f_global = np.concatenate(rows, axis=0)
     pts = block_ridge_pts(ops, state, f_global, sdd_thresh, percentile)
     if world == 1:
         return pts
-    parts = [None] * world
-    dist.all_gather_object(parts, pts, group=group)
-    return np.concatenate(parts, axis=0)
+    return np.concatenate(_all_gather_rows(np.asarray(pts, np.float64), group), axis=0)
 
 
 def block_ridges(ops, state, f_global, sdd_thresh=0.0, percentile=0):
@@ -210,9 +249,9 @@ def sharded_ftle_ridges(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile=0,
     """ftle_ridges of the field's flow map (list of (m, 2) numpy arrays),
     computed by every rank on its row block and joined across the block
     boundaries; identical on every rank to the one-GPU pipeline
-    flowmap_grid_2D -> ftle_evec_2D -> ftle_ridges.  Collectives: two
-    all_gather_object calls on the host (owned FTLE rows, per-rank
-    components)."""
+    flowmap_grid_2D -> ftle_evec_2D -> ftle_ridges.  Collectives: tensor
+    all_gathers of the owned FTLE rows and of the per-rank components
+    (_gather_parts)."""
     import torch.distributed as dist
     ops = ops or GpuOps()
     if dist.is_available() and dist.is_initialized():
@@ -220,15 +259,7 @@ def sharded_ftle_ridges(flow, t0, T, x, y, params, sdd_thresh=0.0, percentile=0,
     else:
         rank, world = 0, 1
     state, owned = block_ftle(ops, rank, world, flow, t0, T, x, y, params, **flowmap_kw)
-    if world == 1:
-        rows = [owned]
-    else:
-        rows = [None] * world
-        dist.all_gather_object(rows, owned, group=group)
+    rows = [owned] if world == 1 else _all_gather_rows(np.asarray(owned, np.float64), group)
     part = block_ridges(ops, state, np.concatenate(rows, axis=0), sdd_thresh, percentile)
-    if world == 1:
-        parts = [part]
-    else:
-        parts = [None] * world
-        dist.all_gather_object(parts, part, group=group)
+    parts = [part] if world == 1 else _gather_parts(part, group)
     return merge_ridges(parts, min_ridge_pts)
