@@ -10,7 +10,7 @@ would have chosen had it known the step's error, log(|h| 0.9 err^(-1/8)).
 Training data come from the integrator itself (:func:`log_steps`); at run
 time ``flowmap_grid_2D(..., precision="mixed", step_model=proposer)`` lets the
 network propose each step while the embedded error estimate still accepts or
-rejects it, so the plain controller remains the fallback and the judge.
+rejects it, so the plain controller remains the fallback and the arbiter.
 """
 import ctypes
 
