@@ -251,6 +251,13 @@ int nbcs_ftle_grid_2d(const double* flowmap, int32_t nx, int32_t ny, double T, d
 int nbcs_c_eig_2d(const double* flowmap, int32_t nx, int32_t ny, double dx, double dy,
                   const uint8_t* mask, double* evals, double* evecs, void* stream);
 
+/* C_tensor_2D (diagnostics.py:69-111): flowmap_aux (nx, ny, naux >= 4, 2) from
+ * nbcs_flowmap_aux_grid_2d -> C (nx,ny,3) = C11, C12, C22 of the Cauchy-Green
+ * tensor of the +-h particles for 2 <= i < nx-2, 2 <= j < ny-2 (unmasked),
+ * 0 elsewhere. */
+int nbcs_c_tensor_2d(const double* flowmap_aux, int32_t nx, int32_t ny, int32_t naux, double h,
+                     const uint8_t* mask, double* C, void* stream);
+
 /* C_eig_aux_2D (diagnostics.py:113-197): flowmap_aux (nx, ny, 5 or 4, 2) from
  * nbcs_flowmap_aux_grid_2d -> evals (nx,ny,2) ascending, evecs (nx,ny,2,2)
  * eigenvectors in columns.  eig_main: eigenvectors from the aux-particle

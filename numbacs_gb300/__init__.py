@@ -6,7 +6,8 @@ signatures.  The compute runs in hand-written CUDA kernels (libnbcs.so, C ABI
 in include/nbcs.h); there is no CPU fallback.
 """
 from . import diagnostics, extraction, flows, integration  # noqa: F401
-from .diagnostics import C_eig_2D, C_eig_aux_2D, ftle_evec_2D, ftle_from_eig, ftle_grid_2D  # noqa: F401
+from .diagnostics import (C_eig_2D, C_eig_aux_2D, C_tensor_2D, ftle_evec_2D,  # noqa: F401
+                          ftle_from_eig, ftle_grid_2D)
 from .extraction import ftle_ordered_ridges, ftle_ridge_pts, ftle_ridges  # noqa: F401
 from .flows import Flow, get_flow_2D, get_interp_arrays_2D, get_predefined_flow  # noqa: F401
 from .integration import (UCGrid, flowmap, flowmap_aux_grid_2D, flowmap_composition,  # noqa: F401

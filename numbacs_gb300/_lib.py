@@ -89,6 +89,7 @@ SIGNATURES = {
                                                 ctypes.POINTER(NbcsOpts), _vp]),
     "nbcs_flowmap_compose": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "nbcs_c_eig_aux_2d": (ctypes.c_int, [_vp, _i32, _i32, _i32, _d, _d, _d, _vp, _vp, _vp, _vp]),
+    "nbcs_c_tensor_2d": (ctypes.c_int, [_vp, _i32, _i32, _i32, _d, _vp, _vp, _vp]),
     "nbcs_ftle_grid_2d": (ctypes.c_int, [_vp, _i32, _i32, _d, _d, _d, _vp, _vp, _vp]),
     "nbcs_c_eig_2d": (ctypes.c_int, [_vp, _i32, _i32, _d, _d, _vp, _vp, _vp, _vp]),
     "nbcs_ftle_from_eig": (ctypes.c_int, [_vp, _i64, _i64, _d, _vp, _vp]),

@@ -124,6 +124,35 @@ __global__ void ceig_kernel(const double2* __restrict__ F, int nx, int ny, doubl
     }
 }
 
+// C_tensor_2D (diagnostics.py:69-111) with utils.gradF_aux_stencil_2D
+// (:50-84): C11, C12, C22 of the tensor of the +-h particles (the first four
+// of the na per point) for 2 <= i < nx-2, 2 <= j < ny-2 unless masked, 0
+// elsewhere -- the stencil of ceig_aux_kernel without the eigen-solve.
+__global__ void ctensor_aux_kernel(const double2* __restrict__ F, int nx, int ny, int na,
+                                   double h, const uint8_t* __restrict__ mask,
+                                   double* __restrict__ C)
+{
+    const long n = (long)nx * ny;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(k / ny), j = (int)(k - (long)i * ny);
+        double c11 = 0.0, c12 = 0.0, c22 = 0.0;
+        if (i >= 2 && i < nx - 2 && j >= 2 && j < ny - 2 && !(mask && mask[k])) {
+            const double2* A = F + k * na;
+            const double dxdx = (A[0].x - A[1].x) / (2.0 * h);
+            const double dxdy = (A[2].x - A[3].x) / (2.0 * h);
+            const double dydx = (A[0].y - A[1].y) / (2.0 * h);
+            const double dydy = (A[2].y - A[3].y) / (2.0 * h);
+            c11 = dxdx * dxdx + dydx * dydx;
+            c12 = dxdx * dxdy + dydx * dydy;
+            c22 = dxdy * dxdy + dydy * dydy;
+        }
+        C[3 * k] = c11;
+        C[3 * k + 1] = c12;
+        C[3 * k + 2] = c22;
+    }
+}
+
 // C_eig_aux_2D (diagnostics.py:113-197) with utils.gradF_aux_stencil_2D
 // (:50-84) and gradF_main_stencil_2D (:88-124): F is (nx, ny, na, 2).
 // eig_main (na = 5): eigenvectors from the aux-particle tensor, eigenvalues
@@ -361,6 +390,22 @@ extern "C" int nbcs_c_eig_aux_2d(const double* flowmap_aux, int32_t nx, int32_t 
     ceig_aux_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
         reinterpret_cast<const double2*>(flowmap_aux), nx, ny, eig_main ? 1 : 0, dx, dy, h, mask,
         reinterpret_cast<double2*>(evals), reinterpret_cast<double2*>(evecs));
+    NBCS_LAUNCH_CHECK();
+    return NBCS_OK;
+}
+
+extern "C" int nbcs_c_tensor_2d(const double* flowmap_aux, int32_t nx, int32_t ny, int32_t naux,
+                                double h, const uint8_t* mask, double* C, void* stream)
+{
+    NBCS_RANGE();
+    if (nx < 0 || ny < 0 || naux < 4)
+        return set_error(NBCS_ERR_INVALID, "c_tensor: negative grid size or fewer than 4 aux particles");
+    long n = (long)nx * ny;
+    if (n == 0) return NBCS_OK;
+    if (!flowmap_aux || !C || (reinterpret_cast<uintptr_t>(flowmap_aux) & 15))
+        return set_error(NBCS_ERR_INVALID, "c_tensor: NULL or misaligned array");
+    ctensor_aux_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(flowmap_aux), nx, ny, naux, h, mask, C);
     NBCS_LAUNCH_CHECK();
     return NBCS_OK;
 }

@@ -1,7 +1,8 @@
 """FTLE diagnostics: the drop-in for the FTLE part of numbacs.diagnostics.
 
-Reference: src/numbacs/diagnostics.py:21-65 (ftle_grid_2D), :113-197
-(C_eig_aux_2D), :200-244 (C_eig_2D) and :247-269 (ftle_from_eig).  Each is one fused stencil kernel
+Reference: src/numbacs/diagnostics.py:21-65 (ftle_grid_2D), :69-111
+(C_tensor_2D), :113-197 (C_eig_aux_2D), :200-244 (C_eig_2D) and :247-269
+(ftle_from_eig).  Each is one fused stencil kernel
 (csrc/ftle.cu).  ``ftle_evec_2D`` is the fused form of the reference idiom
 ``C_eig_2D`` -> ``ftle_from_eig(eigvals[...,1], T)`` / ``eigvecs[...,:,1]`` that
 feeds ridge extraction.
@@ -97,3 +98,21 @@ def C_eig_aux_2D(flowmap_aux, dx, dy, h=1e-5, eig_main=True, mask=None):
                                              float(dy), float(h), D.ptr(md), D.ptr(ev),
                                              D.ptr(vec), D.stream_ptr()))
     return D.finish(ev, as_torch), D.finish(vec, as_torch)
+
+
+def C_tensor_2D(flowmap_aux, dx, dy, h=1e-5, mask=None):
+    """C11, C12, C22 (nx, ny, 3) of the Cauchy-Green tensor from the +-h
+    particles of flowmap_aux_grid_2D's flow map (diagnostics.py:69-111), for
+    2 <= i < nx-2, 2 <= j < ny-2; dx, dy are accepted as the reference does
+    (its stencil does not use them)."""
+    D.require_cuda()
+    as_torch = D.is_torch(flowmap_aux)
+    F = D.to_dev(flowmap_aux)
+    if F.dim() != 4 or F.shape[2] < 4 or F.shape[3] != 2:
+        raise ValueError("flowmap_aux must have shape (nx, ny, 4 or 5, 2)")
+    nx, ny, na = int(F.shape[0]), int(F.shape[1]), int(F.shape[2])
+    md = D.mask_to_dev(mask)
+    C = D.empty((nx, ny, 3))
+    _lib.check(_lib.load().nbcs_c_tensor_2d(D.ptr(F), nx, ny, na, float(h), D.ptr(md), D.ptr(C),
+                                            D.stream_ptr()))
+    return D.finish(C, as_torch)

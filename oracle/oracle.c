@@ -779,6 +779,29 @@ int orc_flowmap_aux_grid_2d(const orc_flow* fl, double t0, double T, const doubl
     return 0;
 }
 
+/* diagnostics.py:69-111 (C_tensor_2D) with utils.gradF_aux_stencil_2D
+ * (:50-84): C11, C12, C22 of the aux-particle tensor for 2 <= i < nx-2,
+ * 2 <= j < ny-2 (unmasked), 0 elsewhere; F is (nx, ny, na, 2). */
+void orc_c_tensor_2d(const double* F, int nx, int ny, int na, double h, const uint8_t* mask,
+                     double* C)
+{
+    memset(C, 0, sizeof(double) * 3 * (size_t)nx * ny);
+    for (int i = 2; i < nx - 2; ++i) {
+        for (int j = 2; j < ny - 2; ++j) {
+            size_t k = (size_t)i * ny + j;
+            if (mask && mask[k]) continue;
+            const double* A = F + k * na * 2;
+            double dxdx = (A[0] - A[2]) / (2.0 * h);
+            double dxdy = (A[4] - A[6]) / (2.0 * h);
+            double dydx = (A[1] - A[3]) / (2.0 * h);
+            double dydy = (A[5] - A[7]) / (2.0 * h);
+            C[3 * k] = dxdx * dxdx + dydx * dydx;
+            C[3 * k + 1] = dxdx * dxdy + dydx * dydy;
+            C[3 * k + 2] = dxdy * dxdy + dydy * dydy;
+        }
+    }
+}
+
 /* diagnostics.py:113-197 (C_eig_aux_2D) with utils.gradF_aux_stencil_2D
  * (:50-84) and gradF_main_stencil_2D (:88-124).  eig_main: eigenvectors from
  * the aux-grid tensor, eigenvalues from the main-grid tensor (centre

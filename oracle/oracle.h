@@ -78,6 +78,10 @@ int orc_flowmap_pts(const orc_flow* flow, double t0, double T, const double* pts
                     const double* params, double rtol, double atol, const uint8_t* mask,
                     double* out, int32_t* status, int nmax, int nthreads);
 
+/* C_tensor_2D: F (nx,ny,na,2) -> C (nx,ny,3) */
+void orc_c_tensor_2d(const double* F, int nx, int ny, int na, double h, const uint8_t* mask,
+                     double* C);
+
 void orc_ftle_grid_2d(const double* fm, int nx, int ny, double T, double dx, double dy,
                       const uint8_t* mask, double* ftle);
 void orc_c_eig_2d(const double* fm, int nx, int ny, double dx, double dy,

@@ -5,6 +5,7 @@ Every function mirrors one reference NumbaCS function on numpy arrays:
   flowmap           src/numbacs/integration.py:8-62
   flowmap_grid_2D   src/numbacs/integration.py:123-182
   ftle_grid_2D      src/numbacs/diagnostics.py:21-65
+  C_tensor_2D       src/numbacs/diagnostics.py:69-111
   C_eig_2D          src/numbacs/diagnostics.py:200-244
   ftle_from_eig     src/numbacs/diagnostics.py:247-269
   ftle_ridge_pts    src/numbacs/extraction/ridges.py:9-76
@@ -84,6 +85,7 @@ def lib():
         L.orc_flowmap_aux_grid_2d.argtypes = [vp, d, d, vp, i, vp, i, vp, d, i, i, d, d, vp, vp,
                                               vp, vp, i, i]
         L.orc_c_eig_aux_2d.argtypes = [vp, i, i, d, d, d, i, vp, vp, vp]
+        L.orc_c_tensor_2d.argtypes = [vp, i, i, i, d, vp, vp]
         L.orc_flowmap_compose.argtypes = [vp, i, i, i, i, vp, vp]
         for fn in (L.orc_cos_deg, L.orc_root8):
             fn.argtypes = [d]
@@ -214,6 +216,16 @@ def flowmap_aux_grid_2D(flow, t0, T, x, y, params, h=1e-5, eig_main=True, comput
     if return_status:
         return out, status, stats
     return out
+
+
+def C_tensor_2D(flowmap_aux, dx, dy, h=1e-5, mask=None):
+    """diagnostics.py:69-111: (nx, ny, 3) C11, C12, C22 from the +-h particles."""
+    F = np.ascontiguousarray(flowmap_aux, np.float64)
+    nx, ny, na = F.shape[:3]
+    C = np.zeros((nx, ny, 3))
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib().orc_c_tensor_2d(_dp(F), nx, ny, na, float(h), _dp(m), _dp(C))
+    return C
 
 
 def C_eig_aux_2D(flowmap_aux, dx, dy, h=1e-5, eig_main=True, mask=None):

@@ -17,6 +17,7 @@ imported here because numba / numbalsoda / interpolation are absent):
   tests/testing_data/fms_cs.npy                                    (tests/test_integration.py:105-114)
   tests/testing_data/fm_aux.npy     flowmap_aux_grid_2D, double gyre 21x11, t0=0, T=8, h=1e-5
                                     (tests/test_integration.py:66-75)
+  tests/testing_data/C.npy          C_tensor_2D(fm_aux, 0.1, 0.1)    (tests/test_diagnostics.py:99-109)
   tests/testing_data/Cevals_aux.npy, C_eig_aux_2D(fm_aux, 0.1, 0.1)  (tests/test_diagnostics.py:112-131)
   tests/testing_data/Cevecs_aux.npy
   tests/testing_data/ordered_ridges.pkl  ftle_ordered_ridges(ftle, Cevecs[...,1], x, y, 0.1)
@@ -99,7 +100,7 @@ def main(ref_root):
     td = os.path.join(ref_root, "tests", "testing_data")
     arrays = {}
     for name in ("fm", "ftle", "Cevals", "Cevecs", "ridge_pts", "fm_ci", "fms_ci", "fm_cs",
-                 "fms_cs", "fm_aux", "Cevals_aux", "Cevecs_aux"):
+                 "fms_cs", "fm_aux", "Cevals_aux", "Cevecs_aux", "C"):
         arrays[name] = np.load(os.path.join(td, name + ".npy"), allow_pickle=False)
     ridges = _load_pkl(os.path.join(td, "ridges.pkl"))
     arrays["n_ridges"] = np.array(len(ridges))

@@ -152,3 +152,17 @@ def test_C_eig_aux_golden_and_oracle(nb, orc, golden, mask_dg):
     assert np.array_equal(ev4, oev4) and np.array_equal(vec4, ovec4)
     with pytest.raises(ValueError):
         nb.C_eig_aux_2D(fa[:, :, :4], 0.1, 0.1)  # eig_main needs the centre particle
+
+
+def test_C_tensor_golden_and_oracle(nb, orc, golden, mask_dg):
+    """C_tensor_2D (diagnostics.py:69-111): the reference's C.npy, plain and
+    masked, and bit-identical to the oracle (4 and 5 aux particles)."""
+    fa = golden["fm_aux"].astype(np.float64)
+    C = nb.C_tensor_2D(fa, 0.1, 0.1)
+    assert np.allclose(C.astype(np.float32), golden["C"])
+    assert np.array_equal(C, orc.C_tensor_2D(fa, 0.1, 0.1))
+    Cm = nb.C_tensor_2D(fa, 0.1, 0.1, mask=mask_dg)
+    assert np.allclose(Cm.astype(np.float32), apply_mask(golden["C"], mask_dg))
+    assert np.array_equal(Cm, orc.C_tensor_2D(fa, 0.1, 0.1, mask=mask_dg))
+    f4 = np.ascontiguousarray(fa[:, :, :4])
+    assert np.array_equal(nb.C_tensor_2D(f4, 0.1, 0.1), orc.C_tensor_2D(f4, 0.1, 0.1))

@@ -460,3 +460,13 @@ def test_flowmap_pts_golden(orc, golden, coords_dg, mask_dg):
     exp[mask_dg] = 0.0
     assert np.allclose(fmm.reshape(len(x), len(y), 2).astype(np.float32), exp)
     assert np.array_equal(st == 1, mask_dg.ravel())
+
+
+def test_C_tensor_2D_golden(orc, golden, mask_dg):
+    """C_tensor_2D of fm_aux.npy (tests/test_diagnostics.py:99-109), plain and masked."""
+    fa = golden["fm_aux"].astype(np.float64)
+    C = orc.C_tensor_2D(fa, 0.1, 0.1)
+    assert np.allclose(C.astype(np.float32), golden["C"])
+    exp = golden["C"].copy()
+    exp[mask_dg] = 0.0
+    assert np.allclose(orc.C_tensor_2D(fa, 0.1, 0.1, mask=mask_dg).astype(np.float32), exp)
