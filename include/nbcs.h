@@ -128,6 +128,17 @@ int nbcs_flowmap_grid_2d(const nbcs_flow* flow, double t0, double T,
                          const uint8_t* mask, double* flowmap, int32_t* status,
                          const nbcs_opts* opts, void* stream);
 
+/* flowmap_n (integration.py:65-121) and flowmap_n_grid_2D (:468-534) with
+ * method="dop853": the positions of each point pts (npts,2) at the n output
+ * times teval (device, params[0] * linspace(t0, t0 + T, n), teval[0] the
+ * start) from one DOP853 run with dop853's dense output, as numbalsoda.dop853
+ * fills a t_eval grid -> out (npts, n, 2); masked points and outputs past a
+ * failure stay 0; status (npts,) may be NULL.  FP64 only (opts may be NULL). */
+int nbcs_flowmap_n_pts(const nbcs_flow* flow, const double* pts, int64_t npts, const double* teval,
+                       int32_t n, const double* params, int32_t np, double rtol, double atol,
+                       const uint8_t* mask, double* out, int32_t* status, const nbcs_opts* opts,
+                       void* stream);
+
 /* flowmap (integration.py:8-62) and flowmap_grid_ND with ndims = 2
  * (:186-247), method="dop853": the same integration for a list of points,
  * pts (npts,2) C-order -> flowmap (npts,2); mask (npts,) u8 and status

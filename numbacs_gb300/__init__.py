@@ -12,6 +12,6 @@ from .extraction import ftle_ordered_ridges, ftle_ridge_pts, ftle_ridges  # noqa
 from .flows import Flow, get_flow_2D, get_interp_arrays_2D, get_predefined_flow  # noqa: F401
 from .integration import (UCGrid, flowmap, flowmap_aux_grid_2D, flowmap_composition,  # noqa: F401
                           flowmap_composition_initial, flowmap_composition_step, flowmap_grid_2D,
-                          flowmap_grid_ND)
+                          flowmap_grid_ND, flowmap_n, flowmap_n_grid_2D)
 
 __version__ = "0.1.0"

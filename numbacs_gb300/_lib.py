@@ -82,6 +82,8 @@ SIGNATURES = {
     "nbcs_eval_rhs": (ctypes.c_int, [_FP, _vp, _i32, _vp, _i64, _vp, _i32, _vp]),
     "nbcs_flowmap_grid_2d": (ctypes.c_int, [_FP, _d, _d, _vp, _i32, _vp, _i32, _vp, _i32, _d, _d,
                                             _vp, _vp, _vp, ctypes.POINTER(NbcsOpts), _vp]),
+    "nbcs_flowmap_n_pts": (ctypes.c_int, [_FP, _vp, _i64, _vp, _i32, _vp, _i32, _d, _d, _vp, _vp,
+                                          _vp, ctypes.POINTER(NbcsOpts), _vp]),
     "nbcs_flowmap_pts": (ctypes.c_int, [_FP, _d, _d, _vp, _i64, _vp, _i32, _d, _d, _vp, _vp, _vp,
                                         ctypes.POINTER(NbcsOpts), _vp]),
     "nbcs_flowmap_aux_grid_2d": (ctypes.c_int, [_FP, _d, _d, _vp, _i32, _vp, _i32, _vp, _i32, _d,

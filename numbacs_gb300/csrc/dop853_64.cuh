@@ -62,19 +62,122 @@ struct Dop853Stats {
     int accepted, rejected, nfcn;
 };
 
+// Dense output (numbalsoda.dop853 with a t_eval grid: dop853's contd8 and its
+// three extra stages) after the accepted step [xold, xold + h] from y0 to y1:
+// stages k1, k6..k12 in slots 0, 5..11 of kc, the derivative at the end in
+// slot 12; the extra stages go to slots 13..15.  Writes the interpolant at
+// every due output time teval[*m] (up to the step's end) to dout[*m].
+template <class Flow, int KS>
+__device__ void dense_output64(const Flow& fl, const Params& P, double xold, double h,
+                               const double* y0, const double* y1, double2* kc,
+                               const double* __restrict__ teval, int n, int* m, double posneg,
+                               double2* __restrict__ dout)
+{
+    double k[17][2];  // 1-based stages (only 1, 6..16 are used)
+#pragma unroll
+    for (int j = 6; j <= 13; ++j) {
+        const double2 v = kc[(j - 1) * KS];
+        k[j][0] = v.x;
+        k[j][1] = v.y;
+    }
+    {
+        const double2 v = kc[0];
+        k[1][0] = v.x;
+        k[1][1] = v.y;
+    }
+    double yy[2], kk[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        yy[i] = y0[i] + h * (DP853_A_14_1 * k[1][i] + DP853_A_14_7 * k[7][i]
+                             + DP853_A_14_8 * k[8][i] + DP853_A_14_9 * k[9][i]
+                             + DP853_A_14_10 * k[10][i] + DP853_A_14_11 * k[11][i]
+                             + DP853_A_14_12 * k[12][i] + DP853_A_14_13 * k[13][i]);
+    fl(xold + DP853_C_14 * h, yy, kk, P);
+    k[14][0] = kk[0];
+    k[14][1] = kk[1];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        yy[i] = y0[i] + h * (DP853_A_15_1 * k[1][i] + DP853_A_15_6 * k[6][i]
+                             + DP853_A_15_7 * k[7][i] + DP853_A_15_8 * k[8][i]
+                             + DP853_A_15_11 * k[11][i] + DP853_A_15_12 * k[12][i]
+                             + DP853_A_15_13 * k[13][i] + DP853_A_15_14 * k[14][i]);
+    fl(xold + DP853_C_15 * h, yy, kk, P);
+    k[15][0] = kk[0];
+    k[15][1] = kk[1];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        yy[i] = y0[i] + h * (DP853_A_16_1 * k[1][i] + DP853_A_16_6 * k[6][i]
+                             + DP853_A_16_7 * k[7][i] + DP853_A_16_8 * k[8][i]
+                             + DP853_A_16_9 * k[9][i] + DP853_A_16_13 * k[13][i]
+                             + DP853_A_16_14 * k[14][i] + DP853_A_16_15 * k[15][i]);
+    fl(xold + DP853_C_16 * h, yy, kk, P);
+    k[16][0] = kk[0];
+    k[16][1] = kk[1];
+    double F[7][2];
+#define NBCS_DENSE_ROW(r)                                                                      \
+    (DP853_D_##r##_1 * k[1][i] + DP853_D_##r##_6 * k[6][i] + DP853_D_##r##_7 * k[7][i]       \
+     + DP853_D_##r##_8 * k[8][i] + DP853_D_##r##_9 * k[9][i] + DP853_D_##r##_10 * k[10][i]   \
+     + DP853_D_##r##_11 * k[11][i] + DP853_D_##r##_12 * k[12][i]                              \
+     + DP853_D_##r##_13 * k[13][i] + DP853_D_##r##_14 * k[14][i]                              \
+     + DP853_D_##r##_15 * k[15][i] + DP853_D_##r##_16 * k[16][i])
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const double d = y1[i] - y0[i];
+        F[0][i] = d;
+        F[1][i] = h * k[1][i] - d;
+        F[2][i] = 2.0 * d - h * (k[13][i] + k[1][i]);
+        F[3][i] = h * NBCS_DENSE_ROW(4);
+        F[4][i] = h * NBCS_DENSE_ROW(5);
+        F[5][i] = h * NBCS_DENSE_ROW(6);
+        F[6][i] = h * NBCS_DENSE_ROW(7);
+    }
+#undef NBCS_DENSE_ROW
+    while (*m < n && (teval[*m] - (xold + h)) * posneg <= 0.0) {
+        const double th = (teval[*m] - xold) / h, th1 = 1.0 - th;
+        double o[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            double v = F[6][i] * th;
+            v = (F[5][i] + v) * th1;
+            v = (F[4][i] + v) * th;
+            v = (F[3][i] + v) * th1;
+            v = (F[2][i] + v) * th;
+            v = (F[1][i] + v) * th1;
+            v = (F[0][i] + v) * th;
+            o[i] = v + y0[i];
+        }
+        dout[*m] = make_double2(o[0], o[1]);
+        ++*m;
+    }
+}
+
 // Integrate y over solver time [x, xend]; `kc` is this thread's shared-memory
 // column of stage derivatives (stride KS, the block size).  Returns NBCS_PARTICLE_*.
-template <class Flow, int KS = kThreads64>
+// DENSE: also the positions at the n output times teval (teval[0] = x,
+// teval[n-1] = xend) into dout[0 .. n), by dense output; kc needs 16 slots.
+// When an output falls in an accepted step, the derivative at its end is
+// evaluated there (for the interpolant) and handed to the next step as its
+// first stage, with the same arguments as that stage would have had, so the
+// step sequence is the one without outputs.
+template <class Flow, int KS = kThreads64, bool DENSE = false>
 __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double xend, double* y,
-                              double rtol, double atol, int nmax, double2* kc, Dop853Stats* st)
+                              double rtol, double atol, int nmax, double2* kc, Dop853Stats* st,
+                              const double* __restrict__ teval = nullptr, int n = 0,
+                              double2* __restrict__ dout = nullptr)
 {
     const double uround = 2.3e-16, safe = 0.9, facc1 = 1.0 / 0.333, facc2 = 1.0 / 6.0;
     const double posneg = (xend - x) >= 0.0 ? 1.0 : -1.0;
     double yy[2], kk[2], h = 0.0, hnew, hmax, err, err2, deno, fac, fac11, sk, erri, sqr;
     bool last = false, reject = false;
     int nstep = 0, status = NBCS_PARTICLE_OK;
+    int m = 1;  // next dense output
     st->accepted = st->rejected = st->nfcn = 0;
-    if (xend == x) return NBCS_PARTICLE_OK;
+    if (DENSE) dout[0] = make_double2(y[0], y[1]);
+    if (xend == x) {
+        if (DENSE)
+            for (; m < n; ++m) dout[m] = make_double2(y[0], y[1]);
+        return NBCS_PARTICLE_OK;
+    }
     hmax = fabs(xend - x);
 
     // HINIT (f0 = f(x, y) is also stage 0 of the first step); one RHS site
@@ -195,10 +298,19 @@ __device__ int dop853_solve64(const Flow& fl, const Params& P, double x, double 
         if (err <= 1.0) {
             st->accepted++;
             st->nfcn++;  // the derivative at the new point (next step's stage 0)
+            bool have_end_derivative = false;
+            if (DENSE && m < n && (teval[m] - (x + h)) * posneg <= 0.0) {
+                fl(x + h, ynew, kk, P);
+                kc[12 * KS] = make_double2(kk[0], kk[1]);
+                dense_output64<Flow, KS>(fl, P, x, h, y, ynew, kc, teval, n, &m, posneg, dout);
+                kc[0] = make_double2(kk[0], kk[1]);
+                st->nfcn += 3;
+                have_end_derivative = true;
+            }
             y[0] = ynew[0];
             y[1] = ynew[1];
             x = x + h;
-            fsal = true;
+            fsal = !have_end_derivative;
             if (last) break;
             if (fabs(hnew) > hmax) hnew = posneg * hmax;
             if (reject) hnew = posneg * dmin_(fabs(hnew), fabs(h));

@@ -87,6 +87,59 @@ struct Launch64 {
     }
 };
 
+// flowmap_n / flowmap_n_grid_2D (integration.py:65-121, :468-534): one thread
+// per point of a list, the positions at the n output times teval by dense
+// output of one DOP853 run (16 stage slots per thread); masked points and the
+// outputs past a failure stay 0.
+constexpr int kDense64Block = 128;
+
+template <class Flow>
+__global__ void __launch_bounds__(kDense64Block)
+flowmap64_n_kernel(Flow fl, Params P, const double* __restrict__ pts, long npts,
+                   const double* __restrict__ teval, int n, const uint8_t* __restrict__ mask,
+                   double2* __restrict__ out, int32_t* __restrict__ status, double rtol,
+                   double atol, int nmax)
+{
+    __shared__ double2 ks[16 * kDense64Block];
+    double2* kc = ks + threadIdx.x;
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npts) return;
+    double2* o = out + k * n;
+    for (int m = 0; m < n; ++m) o[m] = make_double2(0.0, 0.0);
+    int st = NBCS_PARTICLE_MASKED;
+    if (!(mask && mask[k])) {
+        double yv[2] = {pts[2 * k], pts[2 * k + 1]};
+        Dop853Stats s;
+        st = dop853_solve64<Flow, kDense64Block, true>(fl, P, teval[0], teval[n - 1], yv, rtol,
+                                                       atol, nmax, kc, &s, teval, n, o);
+    }
+    if (status) status[k] = st;
+}
+
+struct LaunchDense64 {
+    Params P;
+    const double* pts;
+    long npts;
+    const double* teval;
+    int n;
+    const uint8_t* mask;
+    double* out;
+    int32_t* status;
+    double rtol, atol;
+    int nmax;
+    cudaStream_t stream;
+    template <class Flow>
+    int operator()(const Flow& fl) const
+    {
+        const long blocks = (npts + kDense64Block - 1) / kDense64Block;
+        flowmap64_n_kernel<<<(unsigned)blocks, kDense64Block, 0, stream>>>(
+            fl, P, pts, npts, teval, n, mask, reinterpret_cast<double2*>(out), status, rtol, atol,
+            nmax);
+        NBCS_LAUNCH_CHECK();
+        return NBCS_OK;
+    }
+};
+
 struct LaunchRhs64 {
     Params P;
     const double* ty;
@@ -186,6 +239,38 @@ extern "C" int nbcs_flowmap_pts(const nbcs_flow* flow, double t0, double T, cons
     const AuxGrid list = {kPointList, W, 0, 0.0, (long)npts};
     return flowmap_particles(flow, t0, T, pts, (int32_t)((npts + W - 1) / W), pts, W, params, np,
                              rtol, atol, mask, flowmap, status, opts, stream, list);
+}
+
+extern "C" int nbcs_flowmap_n_pts(const nbcs_flow* flow, const double* pts, int64_t npts,
+                                  const double* teval, int32_t n, const double* params, int32_t np,
+                                  double rtol, double atol, const uint8_t* mask, double* out,
+                                  int32_t* status, const nbcs_opts* opts, void* stream)
+{
+    NBCS_RANGE();
+    int rc = validate_flow(flow, params, np, NBCS_PREC_FP64);
+    if (rc) return rc;
+    if (opts && (opts->precision != NBCS_PREC_FP64 || opts->step_model))
+        return set_error(NBCS_ERR_UNSUPPORTED, "flowmap_n: FP64 only, no step_model");
+    if (npts < 0 || npts > (int64_t)1 << 30 || n < 1)
+        return set_error(NBCS_ERR_INVALID, "flowmap_n: npts in [0, 2^30] and n >= 1");
+    if (npts == 0) return NBCS_OK;
+    if (!pts || !teval || !out || (reinterpret_cast<uintptr_t>(out) & 15))
+        return set_error(NBCS_ERR_INVALID, "flowmap_n: NULL or misaligned array");
+    if (!(rtol > 0.0) || !(atol > 0.0)) return set_error(NBCS_ERR_INVALID, "rtol/atol must be > 0");
+    LaunchDense64 L;
+    for (int i = 0; i < NBCS_MAX_PARAMS; ++i) L.P.v[i] = i < np ? params[i] : 0.0;
+    L.pts = pts;
+    L.npts = (long)npts;
+    L.teval = teval;
+    L.n = n;
+    L.mask = mask;
+    L.out = out;
+    L.status = status;
+    L.rtol = rtol;
+    L.atol = atol;
+    L.nmax = opts && opts->max_steps > 0 ? opts->max_steps : 100000;
+    L.stream = as_stream(stream);
+    return dispatch64(flow, L);
 }
 
 extern "C" int nbcs_flowmap_aux_grid_2d(const nbcs_flow* flow, double t0, double T,

@@ -57,6 +57,18 @@ def main(out=sys.stdout):
         w("#define DP853_E5_%d (%r)\n" % (j, float(E5[j - 1])))
     w("\n#define DP853_BHH1 (%r)\n#define DP853_BHH2 (%r)\n#define DP853_BHH3 (%r)\n"
       % (bhh1, bhh2, bhh3))
+    # dense output (the dop853 code's contd8): stage 13 is the derivative at
+    # the step's end, stages 14..16 the three extra stages (DP853_A_s_j,
+    # DP853_C_s), and DP853_D_r_j (r = 4..7, as the code's d4j..d7j) the
+    # weights of the interpolant's coefficients 4..7 over stages j = 1..16
+    w("\n")
+    for s in range(14, 17):
+        w("#define DP853_C_%d (%r)\n" % (s, float(C[s - 1])))
+        for j in range(1, s):
+            w("#define DP853_A_%d_%d (%r)\n" % (s, j, float(A[s - 1, j - 1])))
+    for r in range(4, 8):
+        for j in range(1, 17):
+            w("#define DP853_D_%d_%d (%r)\n" % (r, j, float(dc.D[r - 4, j - 1])))
     w("\n#endif /* NBCS_DOP853_TABLEAU_H */\n")
 
 

@@ -1,9 +1,10 @@
 """Flow-map integration: the drop-in for numbacs.integration.flowmap_grid_2D,
-flowmap, flowmap_grid_ND, flowmap_aux_grid_2D and the flow-map composition
-functions.
+flowmap, flowmap_n, flowmap_n_grid_2D, flowmap_grid_ND, flowmap_aux_grid_2D
+and the flow-map composition functions.
 
 Reference: src/numbacs/integration.py:123-182 (flowmap_grid_2D), :8-62
-(flowmap), :186-247 (flowmap_grid_ND), :249-464
+(flowmap), :65-121 (flowmap_n), :468-534 (flowmap_n_grid_2D), :186-247
+(flowmap_grid_ND), :249-464
 (flowmap_aux_grid_2D), :609-737 (flowmap_composition, _initial, _step).  The
 reference loops over the particle grid with numba ``prange`` and calls
 numbalsoda's DOP853 per particle; here one CUDA thread (or lane group)
@@ -145,6 +146,71 @@ def flowmap(funcptr, t0, T, pts, params, method="dop853", rtol=1e-6, atol=1e-8, 
     if return_stats:
         res.append(D.finish(stats, as_torch))
     return res[0] if len(res) == 1 else tuple(res)
+
+
+def flowmap_n(funcptr, t0, T, pts, params, method="dop853", n=2, rtol=1e-6, atol=1e-8,
+              mask=None, *, max_steps=100000, return_status=False):
+    """Positions of the points pts (npts, 2) at n times -> ((npts, n, 2), t_eval)
+    (integration.py:65-121): t_eval = params[0] * linspace(t0, t0 + T, n), one
+    DOP853 run per point with dop853's dense output between the steps (as
+    numbalsoda.dop853 fills a t_eval grid), FP64; the returned times are
+    params[0] * t_eval, as the reference returns them."""
+    if method.lower() != "dop853":
+        raise NotImplementedError("method=%r: only 'dop853' is implemented on the GPU" % method)
+    flow = _check_callable_flow(funcptr)
+    if int(n) < 1:
+        raise ValueError("n must be >= 1")
+    D.require_cuda()
+    as_torch = D.is_torch(pts)
+    pd = D.to_dev(pts)
+    if pd.dim() != 2 or pd.shape[1] != 2:
+        raise ValueError("pts must have shape (npts, 2): the flows are two-dimensional")
+    npts = pd.shape[0]
+    md = D.mask_to_dev(mask)
+    if md is not None and tuple(md.shape) != (npts,):
+        raise ValueError("mask must have shape (npts,)")
+    prm = np.ascontiguousarray(
+        params.cpu().numpy() if isinstance(params, torch.Tensor) else params, dtype=np.float64)
+    t_eval = prm[0] * np.linspace(t0, t0 + T, int(n))
+    ted = D.to_dev(np.ascontiguousarray(t_eval))
+    out = D.empty((npts, int(n), 2))
+    status = D.empty((npts,), torch.int32)
+    opts = _lib.NbcsOpts()
+    opts.precision = _lib.PREC_FP64
+    opts.max_steps = int(max_steps)
+    L = _lib.load()
+    _lib.check(L.nbcs_flowmap_n_pts(flow.struct, D.ptr(pd), npts, D.ptr(ted), int(n),
+                                    prm.ctypes.data_as(_lib._vp), len(prm), float(rtol),
+                                    float(atol), D.ptr(md), D.ptr(out), D.ptr(status), opts,
+                                    D.stream_ptr()))
+    if not return_status and not as_torch:
+        _warn_unfinished("flowmap_n", status)
+    res = (D.finish(out, as_torch), prm[0] * t_eval)
+    return res + (D.finish(status, as_torch),) if return_status else res
+
+
+def flowmap_n_grid_2D(funcptr, t0, T, x, y, params, n=50, method="dop853", rtol=1e-6, atol=1e-8,
+                      mask=None, *, max_steps=100000, return_status=False):
+    """flowmap_n over the grid x by y -> ((nx, ny, n, 2), t_eval)
+    (integration.py:468-534), the points in row-major grid order."""
+    D.require_cuda()
+    as_torch = D.is_torch(x, y)
+    xd, yd = D.to_dev(x), D.to_dev(y)
+    nx, ny = xd.numel(), yd.numel()
+    X, Y = torch.meshgrid(xd, yd, indexing="ij")
+    pts = torch.stack([X.reshape(-1), Y.reshape(-1)], dim=1)
+    md = D.mask_to_dev(mask)
+    if md is not None:
+        if tuple(md.shape) != (nx, ny):
+            raise ValueError("mask must have shape (nx, ny)")
+        md = md.reshape(-1)
+    fm, t_eval, st = flowmap_n(funcptr, t0, T, pts, params, method, n, rtol, atol, md,
+                               max_steps=max_steps, return_status=True)
+    fm, st = fm.reshape(nx, ny, int(n), 2), st.reshape(nx, ny)
+    if not return_status and not as_torch:
+        _warn_unfinished("flowmap_n_grid_2D", st)
+    res = (D.finish(fm, as_torch), t_eval)
+    return res + (D.finish(st, as_torch),) if return_status else res
 
 
 def flowmap_grid_ND(funcptr, t0, T, IC_flat, ndims, params, method="dop853", rtol=1e-6,

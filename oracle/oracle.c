@@ -328,8 +328,89 @@ static double hinit(const orc_flow* fl, const double* p, double x, const double*
     return dsign(h, posneg);
 }
 
+/* Dense output of dop853 (its contd8 and the three extra stages, as
+ * numbalsoda.dop853 evaluates a t_eval grid inside one run): after the
+ * accepted step [xold, xold + h] from y0 to y1 with stages k1, k6..k12 and
+ * the derivative k13 at the end, the interpolant at every due output time
+ * teval[*m] (up to the step's end) is written to out[2 * m ..]. */
+static void dense_output(const orc_flow* fl, const double* p, double xold, double h,
+                         const double* y0, const double* y1, const double* k1, const double* k6,
+                         const double* k7, const double* k8, const double* k9, const double* k10,
+                         const double* k11, const double* k12, const double* k13,
+                         const double* teval, int n, int* m, double posneg, double* out)
+{
+    double k14[N2], k15[N2], k16[N2], yy[N2], F[7][N2];
+    for (int i = 0; i < N2; ++i)
+        yy[i] = y0[i] + h * (DP853_A_14_1 * k1[i] + DP853_A_14_7 * k7[i] + DP853_A_14_8 * k8[i]
+                             + DP853_A_14_9 * k9[i] + DP853_A_14_10 * k10[i] + DP853_A_14_11 * k11[i]
+                             + DP853_A_14_12 * k12[i] + DP853_A_14_13 * k13[i]);
+    orc_rhs(fl, xold + DP853_C_14 * h, yy, k14, p);
+    for (int i = 0; i < N2; ++i)
+        yy[i] = y0[i] + h * (DP853_A_15_1 * k1[i] + DP853_A_15_6 * k6[i] + DP853_A_15_7 * k7[i]
+                             + DP853_A_15_8 * k8[i] + DP853_A_15_11 * k11[i] + DP853_A_15_12 * k12[i]
+                             + DP853_A_15_13 * k13[i] + DP853_A_15_14 * k14[i]);
+    orc_rhs(fl, xold + DP853_C_15 * h, yy, k15, p);
+    for (int i = 0; i < N2; ++i)
+        yy[i] = y0[i] + h * (DP853_A_16_1 * k1[i] + DP853_A_16_6 * k6[i] + DP853_A_16_7 * k7[i]
+                             + DP853_A_16_8 * k8[i] + DP853_A_16_9 * k9[i] + DP853_A_16_13 * k13[i]
+                             + DP853_A_16_14 * k14[i] + DP853_A_16_15 * k15[i]);
+    orc_rhs(fl, xold + DP853_C_16 * h, yy, k16, p);
+    for (int i = 0; i < N2; ++i) {
+        double d = y1[i] - y0[i];
+        F[0][i] = d;
+        F[1][i] = h * k1[i] - d;
+        F[2][i] = 2.0 * d - h * (k13[i] + k1[i]);
+#define DENSE_ROW(r) \
+        (DP853_D_##r##_1 * k1[i] + DP853_D_##r##_6 * k6[i] + DP853_D_##r##_7 * k7[i] \
+         + DP853_D_##r##_8 * k8[i] + DP853_D_##r##_9 * k9[i] + DP853_D_##r##_10 * k10[i] \
+         + DP853_D_##r##_11 * k11[i] + DP853_D_##r##_12 * k12[i] + DP853_D_##r##_13 * k13[i] \
+         + DP853_D_##r##_14 * k14[i] + DP853_D_##r##_15 * k15[i] + DP853_D_##r##_16 * k16[i])
+        F[3][i] = h * DENSE_ROW(4);
+        F[4][i] = h * DENSE_ROW(5);
+        F[5][i] = h * DENSE_ROW(6);
+        F[6][i] = h * DENSE_ROW(7);
+#undef DENSE_ROW
+    }
+    while (*m < n && (teval[*m] - (xold + h)) * posneg <= 0.0) {
+        double th = (teval[*m] - xold) / h, th1 = 1.0 - th;
+        for (int i = 0; i < N2; ++i) {
+            double v = F[6][i] * th;
+            v = (F[5][i] + v) * th1;
+            v = (F[4][i] + v) * th;
+            v = (F[3][i] + v) * th1;
+            v = (F[2][i] + v) * th;
+            v = (F[1][i] + v) * th1;
+            v = (F[0][i] + v) * th;
+            out[2 * *m + i] = v + y0[i];
+        }
+        ++*m;
+    }
+}
+
+static int dop853_run(const orc_flow* fl, const double* p, double x, double xend, double* y,
+                      double rtol, double atol, int nmax, int32_t* stats3, const double* teval,
+                      int n, double* dense);
+
 int orc_dop853(const orc_flow* fl, const double* p, double x, double xend,
                double* y, double rtol, double atol, int nmax, int32_t* stats3)
+{
+    return dop853_run(fl, p, x, xend, y, rtol, atol, nmax, stats3, 0, 0, 0);
+}
+
+/* dop853 with dense output at teval[0..n) (teval[0] = x, then in the
+ * direction of integration up to xend): out (n, 2); entries past a failure
+ * stay 0. */
+int orc_dop853_dense(const orc_flow* fl, const double* p, const double* teval, int n, double* y,
+                     double rtol, double atol, int nmax, int32_t* stats3, double* out)
+{
+    memset(out, 0, sizeof(double) * 2 * (size_t)n);
+    if (n < 1) return ORC_OK;
+    return dop853_run(fl, p, teval[0], teval[n - 1], y, rtol, atol, nmax, stats3, teval, n, out);
+}
+
+static int dop853_run(const orc_flow* fl, const double* p, double x, double xend, double* y,
+                      double rtol, double atol, int nmax, int32_t* stats3, const double* teval,
+                      int n, double* dense)
 {
     const double uround = 2.3e-16, safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
     double k1[N2], k2[N2], k3[N2], k4[N2], k5[N2], k6[N2], k7[N2], k8[N2], k9[N2], k10[N2];
@@ -339,9 +420,12 @@ int orc_dop853(const orc_flow* fl, const double* p, double x, double xend,
     double posneg = dsign(1.0, xend - x);
     double hmax, h, hnew, xph, err, err2, deno, fac, fac11, sk, erri, sqr;
     int last = 0, reject = 0, nstep = 0, naccpt = 0, nrejct = 0, nfcn = 0, status = ORC_OK;
+    int m = 1;  /* next dense output */
 
+    if (dense) { dense[0] = y[0]; dense[1] = y[1]; }
     if (xend == x) {
         if (stats3) { stats3[0] = 0; stats3[1] = 0; stats3[2] = 0; }
+        for (; dense && m < n; ++m) { dense[2 * m] = y[0]; dense[2 * m + 1] = y[1]; }
         return ORC_OK;
     }
     orc_rhs(fl, x, y, k1, p);
@@ -432,6 +516,12 @@ int orc_dop853(const orc_flow* fl, const double* p, double x, double xend,
             naccpt++;
             orc_rhs(fl, xph, k5, k4, p);
             nfcn++;
+            /* stages 11 and 12 are in k2 and k3, the end derivative in k4 */
+            if (dense && m < n && (teval[m] - xph) * posneg <= 0.0) {
+                dense_output(fl, p, x, h, y, k5, k1, k6, k7, k8, k9, k10, k2, k3, k4, teval, n,
+                             &m, posneg, dense);
+                nfcn += 3;
+            }
             for (int i = 0; i < N2; ++i) {
                 k1[i] = k4[i];
                 y[i] = k5[i];
@@ -510,6 +600,32 @@ int orc_flowmap_pts(const orc_flow* fl, double t0, double T, const double* pts, 
         int st = orc_dop853(fl, params, ts, te, yv, rtol, atol, nmax, 0);
         out[2 * k] = yv[0];
         out[2 * k + 1] = yv[1];
+        if (status) status[k] = st;
+    }
+    return 0;
+}
+
+/* integration.py:65-121 (flowmap_n, method "dop853"): each point's positions
+ * at the n times teval (params[0] * linspace(t0, t0 + T, n), built by the
+ * caller) from one dense-output run; out (npts, n, 2); masked points and
+ * entries past a failure stay 0. */
+int orc_flowmap_n_pts(const orc_flow* fl, const double* pts, long npts, const double* teval,
+                      int n, const double* params, double rtol, double atol,
+                      const uint8_t* mask, double* out, int32_t* status, int nmax, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (long k = 0; k < npts; ++k) {
+        double* o = out + 2 * (size_t)n * k;
+        if (mask && mask[k]) {
+            memset(o, 0, sizeof(double) * 2 * (size_t)n);
+            if (status) status[k] = ORC_MASKED;
+            continue;
+        }
+        double yv[2] = {pts[2 * k], pts[2 * k + 1]};
+        int st = orc_dop853_dense(fl, params, teval, n, yv, rtol, atol, nmax, 0, o);
         if (status) status[k] = st;
     }
     return 0;

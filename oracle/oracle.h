@@ -73,6 +73,15 @@ int orc_flowmap_grid_2d(const orc_flow* flow, double t0, double T,
                         const uint8_t* mask, double* out, int32_t* status,
                         int32_t* stats, int nmax, int nthreads);
 
+/* dop853 with dense output at teval[0..n): out (n,2) */
+int orc_dop853_dense(const orc_flow* flow, const double* p, const double* teval, int n, double* y,
+                     double rtol, double atol, int nmax, int32_t* stats3, double* out);
+
+/* flowmap_n: pts (npts,2), teval (n) -> out (npts,n,2); mask, status nullable */
+int orc_flowmap_n_pts(const orc_flow* flow, const double* pts, long npts, const double* teval,
+                      int n, const double* params, double rtol, double atol,
+                      const uint8_t* mask, double* out, int32_t* status, int nmax, int nthreads);
+
 /* flowmap: pts (npts,2) -> out (npts,2); mask, status (npts,) nullable */
 int orc_flowmap_pts(const orc_flow* flow, double t0, double T, const double* pts, long npts,
                     const double* params, double rtol, double atol, const uint8_t* mask,

@@ -3,6 +3,7 @@
 Every function mirrors one reference NumbaCS function on numpy arrays:
 
   flowmap           src/numbacs/integration.py:8-62
+  flowmap_n         src/numbacs/integration.py:65-121 (and flowmap_n_grid_2D :468-534)
   flowmap_grid_2D   src/numbacs/integration.py:123-182
   ftle_grid_2D      src/numbacs/diagnostics.py:21-65
   C_tensor_2D       src/numbacs/diagnostics.py:69-111
@@ -75,6 +76,7 @@ def lib():
         L.orc_eval_spline_3d.restype = d
         L.orc_flowmap_grid_2d.argtypes = [vp, d, d, vp, i, vp, i, vp, i, d, d, vp, vp, vp, vp, i, i]
         L.orc_flowmap_pts.argtypes = [vp, d, d, vp, ctypes.c_long, vp, d, d, vp, vp, vp, i, i]
+        L.orc_flowmap_n_pts.argtypes = [vp, vp, ctypes.c_long, vp, i, vp, d, d, vp, vp, vp, i, i]
         L.orc_ftle_grid_2d.argtypes = [vp, i, i, d, d, d, vp, vp]
         L.orc_c_eig_2d.argtypes = [vp, i, i, d, d, vp, vp, vp]
         L.orc_ftle_from_eig.argtypes = [vp, i64, d, vp]
@@ -194,6 +196,36 @@ def flowmap(flow, t0, T, pts, params, rtol=1e-6, atol=1e-8, mask=None, nmax=1000
     lib().orc_flowmap_pts(flow.ptr, float(t0), float(T), _dp(pts), npts, _dp(p), float(rtol),
                           float(atol), _dp(m), _dp(out), _dp(status), int(nmax), int(nthreads))
     return (out, status) if return_status else out
+
+
+def flowmap_n(flow, t0, T, pts, params, n=2, rtol=1e-6, atol=1e-8, mask=None, nmax=100000,
+              nthreads=0, return_status=False):
+    """integration.py:65-121 (method dop853): pts (npts, 2) -> ((npts, n, 2), t_eval), the
+    positions at t_eval = params[0] * linspace(t0, t0 + T, n) by dense output of one run."""
+    pts = np.ascontiguousarray(pts, np.float64)
+    p = np.ascontiguousarray(params, np.float64)
+    te = np.ascontiguousarray(p[0] * np.linspace(t0, t0 + T, n))
+    npts = pts.shape[0]
+    out = np.zeros((npts, n, 2))
+    status = np.zeros(npts, np.int32)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    lib().orc_flowmap_n_pts(flow.ptr, _dp(pts), npts, _dp(te), int(n), _dp(p), float(rtol),
+                            float(atol), _dp(m), _dp(out), _dp(status), int(nmax), int(nthreads))
+    res = (out, p[0] * te)
+    return res + (status,) if return_status else res
+
+
+def flowmap_n_grid_2D(flow, t0, T, x, y, params, n=50, rtol=1e-6, atol=1e-8, mask=None,
+                      nmax=100000, nthreads=0, return_status=False):
+    """integration.py:468-534: the grid's points through flowmap_n -> ((nx, ny, n, 2), t_eval)."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    m = None if mask is None else np.asarray(mask).ravel()
+    r = flowmap_n(flow, t0, T, np.column_stack((X.ravel(), Y.ravel())), params, n, rtol, atol, m,
+                  nmax, nthreads, return_status)
+    out = (r[0].reshape(len(x), len(y), n, 2), r[1])
+    return out + (r[2].reshape(len(x), len(y)),) if return_status else out
 
 
 def flowmap_aux_grid_2D(flow, t0, T, x, y, params, h=1e-5, eig_main=True, compute_edge=True,

@@ -6,6 +6,8 @@ imported here because numba / numbalsoda / interpolation are absent):
 
   tests/testing_data/fm.npy         flowmap_grid_2D, double gyre 21x11, t0=0, T=8
                                     (tests/test_integration.py:55-64)
+  tests/testing_data/fm_n.npy       flowmap_n / flowmap_n_grid_2D, the same particles at n = 4
+                                    times (tests/test_integration.py:45-52, :78-90)
   tests/testing_data/ftle.npy       ftle_grid_2D(fm, 8, 0.1, 0.1)  (tests/test_diagnostics.py:82-96)
   tests/testing_data/Cevals.npy,    C_eig_2D(fm, 0.1, 0.1)           (tests/test_diagnostics.py:133-150)
   tests/testing_data/Cevecs.npy
@@ -100,7 +102,7 @@ def main(ref_root):
     td = os.path.join(ref_root, "tests", "testing_data")
     arrays = {}
     for name in ("fm", "ftle", "Cevals", "Cevecs", "ridge_pts", "fm_ci", "fms_ci", "fm_cs",
-                 "fms_cs", "fm_aux", "Cevals_aux", "Cevecs_aux", "C"):
+                 "fms_cs", "fm_aux", "Cevals_aux", "Cevecs_aux", "C", "fm_n"):
         arrays[name] = np.load(os.path.join(td, name + ".npy"), allow_pickle=False)
     ridges = _load_pkl(os.path.join(td, "ridges.pkl"))
     arrays["n_ridges"] = np.array(len(ridges))

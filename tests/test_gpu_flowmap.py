@@ -408,3 +408,44 @@ def test_flowmap_pts(nb, orc, golden, coords_dg, mask_dg):
     tp = torch.from_numpy(sp).cuda()
     ft = nb.flowmap(sfl, 24.0, -18.0, tp, ps, mask=torch.from_numpy(sm).cuda())
     assert ft.is_cuda and torch.equal(ft.cpu(), torch.from_numpy(f64))
+
+
+def test_flowmap_n(nb, orc, golden, coords_dg, mask_dg):
+    """flowmap_n / flowmap_n_grid_2D (integration.py:65-121, :468-534) by
+    dense output: the reference's fm_n.npy, plain and masked; the last output
+    is flowmap_grid_2D's end point; a spline flow bit-identical to the oracle,
+    forward and backward, including T = 0 and n = 1."""
+    x, y = coords_dg
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    pts = np.column_stack((X.ravel(), Y.ravel()))
+    fl, p, _ = nb.get_predefined_flow("double_gyre")
+    fm_n, te = nb.flowmap_n(fl, 0.0, 8.0, pts, p, n=4)
+    assert np.allclose(te, p[0] * np.linspace(0.0, 8.0, 4))
+    assert np.allclose(fm_n.reshape(21, 11, 4, 2).astype(np.float32), golden["fm_n"])
+    g, te2 = nb.flowmap_n_grid_2D(fl, 0.0, 8.0, x, y, p, n=4)
+    assert np.array_equal(g, fm_n.reshape(21, 11, 4, 2)) and np.array_equal(te, te2)
+    # the interpolant at the end is (y1 - y0) + y0: y1 up to one rounding
+    assert np.abs(g[:, :, -1] - nb.flowmap_grid_2D(fl, 0.0, 8.0, x, y, p)).max() <= 1e-15
+    gm, _, st = nb.flowmap_n_grid_2D(fl, 0.0, 8.0, x, y, p, n=4, mask=mask_dg,
+                                      return_status=True)
+    assert np.allclose(gm.astype(np.float32), apply_mask(golden["fm_n"], mask_dg))
+    assert np.array_equal(st == 1, mask_dg)
+    # spline flow: the same arithmetic as the oracle
+    tv, lon, lat = np.arange(9) * 3.0, np.linspace(-20.0, 20.0, 11), np.linspace(0.0, 30.0, 9)
+    T3, X3, Y3 = np.meshgrid(tv, lon, lat, indexing="ij")
+    U = 30.0 * np.sin(0.15 * X3 + 0.05 * T3) * np.cos(0.1 * Y3)
+    V = 20.0 * np.cos(0.12 * X3) * np.sin(0.2 * Y3 - 0.03 * T3)
+    grid, Cu, Cv = nb.get_interp_arrays_2D(tv, lon, lat, U, V)
+    sfl = nb.get_flow_2D(grid, Cu, Cv, spherical=1)
+    og, oCu, oCv = orc.get_interp_arrays_2D(tv, lon, lat, U, V)
+    ofl = orc.spline_flow(og, oCu, oCv, spherical=1)
+    rng = np.random.default_rng(5)
+    sp = np.column_stack((rng.uniform(-25.0, 25.0, 301), rng.uniform(-2.0, 32.0, 301)))
+    ps = np.array([-1.0])
+    for t0, T, n in ((24.0, -18.0, 7), (3.0, 20.0, 5), (10.0, 0.0, 3), (10.0, 5.0, 1)):
+        a, ta, sa = nb.flowmap_n(sfl, t0, T, sp, ps, n=n, return_status=True)
+        b, tb, sb = orc.flowmap_n(ofl, t0, T, sp, ps, n=n, return_status=True)
+        assert np.array_equal(a, b) and np.array_equal(ta, tb) and np.array_equal(sa, sb), (t0, T)
+    # torch in, torch out
+    at, _ = nb.flowmap_n(sfl, 24.0, -18.0, torch.from_numpy(sp).cuda(), ps, n=7)
+    assert at.is_cuda and torch.equal(at.cpu(), torch.from_numpy(nb.flowmap_n(sfl, 24.0, -18.0, sp, ps, n=7)[0]))

@@ -470,3 +470,24 @@ def test_C_tensor_2D_golden(orc, golden, mask_dg):
     exp = golden["C"].copy()
     exp[mask_dg] = 0.0
     assert np.allclose(orc.C_tensor_2D(fa, 0.1, 0.1, mask=mask_dg).astype(np.float32), exp)
+
+
+def test_flowmap_n_golden(orc, golden, coords_dg, mask_dg):
+    """flowmap_n / flowmap_n_grid_2D (tests/test_integration.py:45-52, :78-90):
+    dop853's dense output over one run reproduces fm_n.npy, plain and masked;
+    the last output is flowmap_grid_2D's end point."""
+    x, y = coords_dg
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    pts = np.column_stack((X.ravel(), Y.ravel()))
+    dg = orc.double_gyre()
+    p = np.array([1.0, 0.1, 0.25, 0.0, 0.2 * np.pi, 0.0])
+    fm_n, te = orc.flowmap_n(dg, 0.0, 8.0, pts, p, n=4)
+    assert np.allclose(te, p[0] * np.linspace(0.0, 8.0, 4))
+    assert np.allclose(fm_n.reshape(21, 11, 4, 2).astype(np.float32), golden["fm_n"])
+    g, _ = orc.flowmap_n_grid_2D(dg, 0.0, 8.0, x, y, p, n=4)
+    assert np.array_equal(g, fm_n.reshape(21, 11, 4, 2))
+    assert np.array_equal(g[:, :, -1], orc.flowmap_grid_2D(dg, 0.0, 8.0, x, y, p))
+    gm, _ = orc.flowmap_n_grid_2D(dg, 0.0, 8.0, x, y, p, n=4, mask=mask_dg)
+    exp = golden["fm_n"].copy()
+    exp[mask_dg] = 0.0
+    assert np.allclose(gm.astype(np.float32), exp)
