@@ -21,7 +21,6 @@ single-GPU legs run only when N = 1.
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess

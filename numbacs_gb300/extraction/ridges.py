@@ -6,7 +6,6 @@ compaction pipeline on the GPU (csrc/ridges.cu).  The threshold is the
 reference's ``np.percentile(f, percentile)`` as numba evaluates it, or 0 when
 ``percentile == 0``.
 """
-import numpy as np
 import torch
 
 from .. import _device as D

@@ -11,7 +11,6 @@ This file is named so that pytest collects it last.
 """
 import ctypes
 
-import numpy as np
 import pytest
 import torch
 
