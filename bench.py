@@ -573,7 +573,8 @@ def run_ours(args, rank, world):
     if not args.no_e2e and not args.quick:
         out["e2e"] = run_e2e(nb, D, wl, prec, rtol, atol, args, world)
         _leg("e2e", out)
-    if not args.no_cpu_baseline and not args.quick and rank == 0:
+    # the CPU baseline: rank 0 at N = 1 only (a scaling run would hold every GPU idle)
+    if not args.no_cpu_baseline and not args.quick and solo:
         out["cpu_baseline"] = run_cpu_baseline(wl, rtol, atol, args.cpu_seconds, value_gpu=value,
                                                truth=truth)
         _leg("cpu_baseline", out)
